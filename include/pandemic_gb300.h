@@ -1,0 +1,150 @@
+/*
+ * pandemic_gb300.h - C ABI of the GB300-native PandemicThrust daily simulation step.
+ *
+ * The reference has no plugin or FFI layer: its boundary is class PandemicSim
+ * (PandemicThrust/PandemicThrust/PandemicSim.h:68-281) driven by main.cu:19-21,
+ * plus the file contract constants.csv + seed.txt -> output_infected_stats.csv,
+ * output_rn.csv, infected_max.txt.  Each entry point below names the reference
+ * member or routine it replaces.  All pointers are host pointers; the library
+ * owns every device buffer and never keeps a caller pointer after returning.
+ *
+ * A pt_sim is not thread-safe.  Its work runs on one CUDA stream (the caller's, or
+ * one it creates).  Results do not depend on the stream, grid shape or GPU.
+ */
+#ifndef PANDEMIC_GB300_H
+#define PANDEMIC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pt_status {
+    PT_OK = 0,
+    PT_DONE = 1,          /* the infected count reached zero: the reference breaks its day loop */
+    PT_FINISHED = 2,      /* max_days simulated */
+    PT_ERR_ARG = -1,      /* invalid argument or parameter value */
+    PT_ERR_IO = -2,       /* a file could not be opened */
+    PT_ERR_PARSE = -3,    /* a file could not be parsed */
+    PT_ERR_OOM = -4,      /* device or host allocation failed */
+    PT_ERR_CUDA = -5,     /* a CUDA call or kernel failed */
+    PT_ERR_STATE = -6,    /* call out of order (e.g. step before setup) */
+    PT_ERR_TIMEOUT = -7   /* a device-side wait gave up; see pt_last_error */
+} pt_status;
+
+/* The nine numeric columns of constants.csv, in file order
+ * (PandemicSim.cu:299-309; PandemicSim::setup_loadParameters). */
+typedef struct pt_params {
+    int   max_days;              /* 0..255: the reference's day counter is 8-bit */
+    float r_pandemic;
+    float r_seasonal;
+    int   initial_pandemic;
+    int   initial_seasonal;
+    float people_scaling;        /* households = round(people_scaling * 1e6) */
+    float location_scaling;      /* scales the 14 business-type counts */
+    float percent_symptomatic;
+    float asymp_factor;
+} pt_params;
+
+/* Sizes and derived values of a created (and set-up) simulation. */
+typedef struct pt_info {
+    int number_people;           /* 0 until pt_setup */
+    int number_households;
+    int number_workplaces;
+    int number_adults;
+    int number_children;
+    int current_day;             /* next day to simulate */
+    int days_run;                /* rows written to the daily statistics */
+    int infected_count;          /* infected count of the last day counted */
+    uint64_t rand_offset;        /* the reference's global Random123 counter */
+    int seeds[4];                /* SEED_HOST after srand(core_seed) (PandemicSim.cu:2856-2861) */
+    int type_count[14];
+    int type_offset[14];
+    float infectiousness[2];
+    int max_day_of_peak;         /* day with the largest infected proportion */
+    float max_infected_proportion;
+    int sm_count;
+    uint64_t device_bytes;       /* device memory held by this simulation */
+} pt_info;
+
+typedef struct pt_sim pt_sim;
+
+/* PandemicSim::setup_loadParameters (PandemicSim.cu:286-310): the reference's
+ * positional fscanf parse of constants.csv. */
+pt_status pt_params_from_csv(const char *path, pt_params *out);
+
+/* PandemicSim::setup_loadSeed (PandemicSim.cu:2843-2862): one int from seed.txt. */
+pt_status pt_seed_from_file(const char *path, int *core_seed);
+
+/* PandemicSim::PandemicSim() (PandemicSim.cu:98-133): seeds, scaling
+ * (setup_scaleSimulation, :1127-1162), infection data (:2828-2840) and device
+ * constants.  cuda_stream is a cudaStream_t or NULL for a library-owned stream. */
+pt_status pt_create(const pt_params *params, int core_seed, void *cuda_stream, pt_sim **out);
+
+/* PandemicSim::setupSim (PandemicSim.cu:146-208): population, households,
+ * workplaces and schools, workplace table, status arrays, initial infected. */
+pt_status pt_setup(pt_sim *sim);
+
+/* One iteration of PandemicSim::runToCompletion (PandemicSim.cu:882-954):
+ * daily_countAndRecover, daily_buildInfectedArray_global and, when anyone is
+ * infected, doWeekday_wholeDay or doWeekend_wholeDay.  counts16 (may be NULL)
+ * receives the 8 pandemic then 8 seasonal status bins counted before the day's
+ * contacts (status_counts_today, :2760).  Returns PT_OK, PT_DONE when the
+ * infected count was zero (no contacts ran, as the reference's break at :900) or
+ * PT_FINISHED when max_days days have run.  Synchronises the stream. */
+pt_status pt_step_day(pt_sim *sim, int counts16[16], int *infected_count);
+
+/* PandemicSim::runToCompletion without per-day host synchronisation: runs the
+ * remaining days on the device (captured as one CUDA graph) and copies back, per
+ * day, the 16 status bins (counts, max_days*16 ints, may be NULL) and the
+ * infected count (infected, max_days ints, may be NULL).  days_run receives the
+ * number of statistics rows, as the reference's output_infected_stats.csv. */
+pt_status pt_run(pt_sim *sim, int *counts, int *infected, int *days_run);
+
+/* final_countReproduction (PandemicSim.cu:2227-2304): the number of persons per
+ * generation value 0..255, for each strain (256 ints each). */
+pt_status pt_final_gen_counts(pt_sim *sim, int gen_p[256], int gen_s[256]);
+
+/* Resets the epidemic to the state right after pt_setup (status arrays, initial
+ * infected, counters) without regenerating the population.  Used to repeat a run. */
+pt_status pt_reset_epidemic(pt_sim *sim);
+
+pt_status pt_get_info(const pt_sim *sim, pt_info *out);
+
+/* Copies per-person state to host buffers (any may be NULL; each holds N entries):
+ * status and day per strain, generation per strain, age code. */
+pt_status pt_get_person_state(pt_sim *sim, uint8_t *status_p, uint8_t *status_s,
+                              uint8_t *day_p, uint8_t *day_s, uint8_t *gen_p, uint8_t *gen_s,
+                              uint8_t *age);
+
+/* Copies setup tables: person -> household (N), household offsets (H+1), person ->
+ * workplace or school (N), workplace people (N), workplace offsets (L+1). */
+pt_status pt_get_population(pt_sim *sim, int32_t *household, int32_t *household_offset,
+                            int32_t *workplace, int32_t *workplace_people,
+                            int32_t *workplace_offset);
+
+/* Copies the last built day's tables: infected list (infected_count entries),
+ * schedule keys and bucketed person ids (2N weekday / 3N weekend) and bucket
+ * offsets (2L+1 / 10L+1).  entries and buckets receive the sizes. */
+pt_status pt_get_day_tables(pt_sim *sim, int32_t *infected, int32_t *keys, int32_t *people,
+                            int32_t *offsets, int *entries, int *buckets);
+
+/* Milliseconds of device time per stage accumulated since the last call (CUDA
+ * events on the simulation's stream; enabled by pt_set_timing).  Stages:
+ * 0 sweep, 1 schedule, 2 bucket build, 3 infection, 4 apply. */
+pt_status pt_set_timing(pt_sim *sim, int enabled);
+pt_status pt_get_stage_ms(pt_sim *sim, float ms[8]);
+
+/* Kernel launches issued by this library in the calling process so far. */
+uint64_t pt_launch_count(void);
+
+void pt_destroy(pt_sim *sim);
+
+/* Text of the last error on sim (or of the last failed pt_create when sim is NULL). */
+const char *pt_last_error(const pt_sim *sim);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

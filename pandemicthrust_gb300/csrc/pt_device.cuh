@@ -1,0 +1,268 @@
+// pt_device.cuh - device-side building blocks of the daily simulation step:
+// Threefry counters, the float "fishing" lookups and the model tables.
+//
+// Every float operation that decides a result uses an explicit round-to-nearest
+// intrinsic (__fmul_rn, __fdiv_rn, __fsub_rn, __uint2float_rn), so the arithmetic
+// matches the reference's IEEE single-precision code whatever the compiler flags
+// (no contraction, no approximate division).
+#pragma once
+#include <cstdint>
+#include "pt_kernels.h"
+
+namespace ptk {
+
+// ---------------------------------------------------------------- tables
+// PandemicSim.cu:328-481 (model constants; identical in every simulation).
+__constant__ float c_child_age_cdf[5] = {0.24f, 0.47f, 0.72f, 0.85f, 1.0f};
+__constant__ float c_workplace_pdf[kTypes] = {
+    0.06586f, 0.05802f, 0.30227f, 0.0048f, 0.00997f, 0.203f, 0.09736f,
+    0.10598f, 0.00681f, 0.02599f, 0.f, 0.08749f, 0.03181f, 0.00064f};
+__constant__ int c_type_max_contacts[kTypes] = {3, 3, 3, 2, 2, 3, 3, 2, 2, 2, 0, 2, 2, 2};
+__constant__ float c_weekday_errand_pdf[kTypes] = {0, 0, 0, 0, 0, 0, 0, 0, 0,
+                                                   0.61919f, 0, 0.27812f, 0.06601f, 0.03668f};
+__constant__ float c_weekend_errand_pdf[kTypes] = {0, 0, 0, 0, 0, 0, 0, 0, 0,
+                                                   0.51493f, 0, 0.25586f, 0.1162f, 0.113f};
+__constant__ int c_hh_adults[9] = {1, 1, 2, 1, 2, 1, 2, 1, 2};
+__constant__ int c_hh_children[9] = {0, 1, 0, 2, 1, 3, 2, 4, 3};
+__constant__ float c_hh_cdf[9] = {0.279f, 0.319f, 0.628f, 0.671f, 0.8f, 0.812f, 0.939f, 0.944f, 1.0f};
+// Contacts per errand hour for weekday profiles 0..3 (3 = afterschool) and the
+// errand slot of each of the two weekend errand contacts (PandemicSim.cu:445-481).
+__constant__ int c_weekday_assign[4][2] = {{2, 0}, {0, 2}, {1, 1}, {2, 0}};
+__constant__ int c_weekend_assign[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+
+// ---------------------------------------------------------------- Threefry
+// Threefry-2x64-20 and 2x32-20 (Salmon et al., SC'11; the Random123 rotation
+// tables).  64-bit words are handled as 32-bit halves so each rotation is two
+// funnel shifts and each add an add/add-with-carry pair.
+struct u64h { uint32_t lo, hi; };
+
+__device__ __forceinline__ u64h mk(uint64_t v) { return {(uint32_t)v, (uint32_t)(v >> 32)}; }
+
+__device__ __forceinline__ u64h add64(u64h a, u64h b)
+{
+    u64h r;
+    asm("add.cc.u32 %0, %2, %4;\n\taddc.u32 %1, %3, %5;"
+        : "=r"(r.lo), "=r"(r.hi) : "r"(a.lo), "r"(a.hi), "r"(b.lo), "r"(b.hi));
+    return r;
+}
+
+template <int R>
+__device__ __forceinline__ u64h rotl64(u64h x)
+{
+    if constexpr (R == 32) {
+        return {x.hi, x.lo};
+    } else if constexpr (R < 32) {
+        return {__funnelshift_l(x.hi, x.lo, R), __funnelshift_l(x.lo, x.hi, R)};
+    } else {
+        return {__funnelshift_l(x.lo, x.hi, R - 32), __funnelshift_l(x.hi, x.lo, R - 32)};
+    }
+}
+
+template <int R>
+__device__ __forceinline__ void mix64(u64h &x0, u64h &x1)
+{
+    x0 = add64(x0, x1);
+    x1 = rotl64<R>(x1);
+    x1.lo ^= x0.lo;
+    x1.hi ^= x0.hi;
+}
+
+struct TfKey {
+    u64h k0, k1, k2;       // key schedule: k2 = parity ^ k0 ^ k1
+    uint32_t k32_0, k32_1, k32_2;
+};
+
+__device__ __forceinline__ TfKey make_key(const SimConst &c)
+{
+    TfKey k;
+    k.k0 = mk(c.key0);
+    k.k1 = mk(c.key1);
+    k.k2 = mk(0x1BD11BDAA9FC1A22ULL ^ c.key0 ^ c.key1);
+    k.k32_0 = (uint32_t)c.key0;
+    k.k32_1 = (uint32_t)c.key1;
+    k.k32_2 = 0x1BD11BDAu ^ k.k32_0 ^ k.k32_1;
+    return k;
+}
+
+// Counter {ctr, ctr}; returns the block as the reference's union reads it:
+// w[0] = lo(x0), w[1] = hi(x0), w[2] = lo(x1), w[3] = hi(x1).
+__device__ __forceinline__ void tf2x64(const TfKey &k, uint64_t ctr, uint32_t w[4])
+{
+    u64h c = mk(ctr);
+    u64h x0 = add64(c, k.k0);
+    u64h x1 = add64(c, k.k1);
+    const u64h ks[3] = {k.k0, k.k1, k.k2};
+#pragma unroll
+    for (int blk = 0; blk < 5; blk++) {
+        if ((blk & 1) == 0) {
+            mix64<16>(x0, x1); mix64<42>(x0, x1); mix64<12>(x0, x1); mix64<31>(x0, x1);
+        } else {
+            mix64<16>(x0, x1); mix64<32>(x0, x1); mix64<24>(x0, x1); mix64<21>(x0, x1);
+        }
+        const int s = blk + 1;
+        x0 = add64(x0, ks[s % 3]);
+        x1 = add64(x1, add64(ks[(s + 1) % 3], u64h{(uint32_t)s, 0u}));
+    }
+    w[0] = x0.lo; w[1] = x0.hi; w[2] = x1.lo; w[3] = x1.hi;
+}
+
+template <int R>
+__device__ __forceinline__ void mix32(uint32_t &x0, uint32_t &x1)
+{
+    x0 += x1;
+    x1 = __funnelshift_l(x1, x1, R);
+    x1 ^= x0;
+}
+
+__device__ __forceinline__ void tf2x32(const TfKey &k, uint32_t ctr, uint32_t w[2])
+{
+    uint32_t x0 = ctr + k.k32_0, x1 = ctr + k.k32_1;
+    const uint32_t ks[3] = {k.k32_0, k.k32_1, k.k32_2};
+#pragma unroll
+    for (int blk = 0; blk < 5; blk++) {
+        if ((blk & 1) == 0) {
+            mix32<13>(x0, x1); mix32<15>(x0, x1); mix32<26>(x0, x1); mix32<6>(x0, x1);
+        } else {
+            mix32<17>(x0, x1); mix32<29>(x0, x1); mix32<16>(x0, x1); mix32<24>(x0, x1);
+        }
+        const uint32_t s = blk + 1;
+        x0 += ks[s % 3];
+        x1 += ks[(s + 1) % 3] + s;
+    }
+    w[0] = x0; w[1] = x1;
+}
+
+// ---------------------------------------------------------------- fishing
+// (float)r / UNSIGNED_MAX: the divisor converts to 2^32, so this is exact scaling.
+__device__ __forceinline__ float to_unit(uint32_t r) { return __fmul_rn(__uint2float_rn(r), 0x1p-32f); }
+
+// device_setup_fishHouseholdType, PandemicSim.cu:2360-2371
+__device__ __forceinline__ int fish_household_type(uint32_t r)
+{
+    float y = to_unit(r);
+    int row = 0;
+    while (y > c_hh_cdf[row] && row < 8) row++;
+    return row;
+}
+
+__device__ __forceinline__ int business_in_type(const SimConst &c, float frac, int type)
+{
+    int count = c.type_count[type];
+    int b = __float2int_rz(__fmul_rn(frac, __int2float_rn(count)));
+    if (b >= count) b = count - 1;
+    return b + c.type_offset[type];
+}
+
+// device_setup_fishWorkplace, PandemicSim.cu:2374-2399
+__device__ __forceinline__ int fish_workplace(const SimConst &c, uint32_t r)
+{
+    float y = to_unit(r);
+    int row = 0;
+    while (c_workplace_pdf[row] < y && row < kTypes - 1) {
+        y = __fsub_rn(y, c_workplace_pdf[row]);
+        row++;
+    }
+    return business_in_type(c, __fdiv_rn(y, c_workplace_pdf[row]), row);
+}
+
+// device_setup_fishSchoolAndAge, PandemicSim.cu:2402-2442
+__device__ __forceinline__ int fish_school_and_age(const SimConst &c, uint32_t r, int *age)
+{
+    float y = to_unit(r);
+    int row = 0;
+    while (row < 4 && y > c_child_age_cdf[row]) row++;
+    float frac;
+    if (row == 0) {
+        frac = __fdiv_rn(y, c_child_age_cdf[0]);
+    } else {
+        float pdf_here = __fsub_rn(c_child_age_cdf[row], c_child_age_cdf[row - 1]);
+        float y_here = __fsub_rn(y, c_child_age_cdf[row - 1]);
+        frac = __fdiv_rn(y_here, pdf_here);
+    }
+    *age = row;
+    return business_in_type(c, frac, row + 3);
+}
+
+// device_fishAfterschoolOrErrandDestination_weekday, PandemicSim.cu:2909-2947
+// (unsigned business number, as the reference).
+__device__ __forceinline__ int fish_weekday_dest(const SimConst &c, uint32_t r, bool adult)
+{
+    int type = 8;  // BUSINESS_TYPE_AFTERSCHOOL
+    float frac = to_unit(r);
+    if (adult) {
+        type = 9;
+        float row_pdf = c_weekday_errand_pdf[type];
+        while (frac > row_pdf && type < kTypes - 1) {
+            frac = __fsub_rn(frac, row_pdf);
+            type++;
+            row_pdf = c_weekday_errand_pdf[type];
+        }
+        frac = __fdiv_rn(frac, row_pdf);
+    }
+    int count = c.type_count[type];
+    unsigned int b = __float2uint_rz(__fmul_rn(frac, __int2float_rn(count)));
+    if (b >= (unsigned int)count) b = (unsigned int)(count - 1);
+    b += (unsigned int)c.type_offset[type];
+    return (int)b;
+}
+
+// device_fishWeekendErrandDestination, PandemicSim.cu:1017-1044
+__device__ __forceinline__ int fish_weekend_dest(const SimConst &c, uint32_t r)
+{
+    float y = to_unit(r);
+    int row = 9;
+    while (y > c_weekend_errand_pdf[row] && row < kTypes - 1) {
+        y = __fsub_rn(y, c_weekend_errand_pdf[row]);
+        row++;
+    }
+    return business_in_type(c, __fdiv_rn(y, c_weekend_errand_pdf[row]), row);
+}
+
+// device_generateWeekendErrands, PandemicSim.cu:980-1014: three distinct hours of
+// ten, each with a destination; key = destination + hour * L.
+__device__ __forceinline__ void weekend_errands(const SimConst &c, const TfKey &k, uint64_t ctr, int out[3])
+{
+    uint32_t w[8];
+    tf2x64(k, ctr, w);
+    tf2x64(k, ctr + 1, w + 4);
+    int h1 = (int)(w[0] % 10u);
+    int h2 = (int)(w[1] % 10u);
+    if (h2 == h1) h2 = (h2 + 1) % 10;
+    int h3 = (int)(w[2] % 10u);
+    while (h3 == h1 || h3 == h2) h3 = (h3 + 1) % 10;
+    out[0] = fish_weekend_dest(c, w[3]) + h1 * c.L;
+    out[1] = fish_weekend_dest(c, w[4]) + h2 * c.L;
+    out[2] = fish_weekend_dest(c, w[5]) + h3 * c.L;
+}
+
+// device_getWorkplaceMaxContacts, PandemicSim.cu:3492-3511
+__device__ __forceinline__ int workplace_max_contacts(const SimConst &c, int loc)
+{
+    int lid = loc % c.L;
+    int t = 0, off, cnt, mx;
+    do {
+        off = c.type_offset[t];
+        cnt = c.type_count[t];
+        mx = c_type_max_contacts[t];
+        t++;
+    } while (lid >= off + cnt);
+    return mx;
+}
+
+// device_getInfectionProfile, PandemicSim.cu:3974-3988
+__device__ __forceinline__ int infection_profile(const SimConst &c, uint32_t r)
+{
+    int p = (int)(r % 3u) + 2;
+    if (to_unit(r) > c.pct_sympt) p += 3;
+    return p;
+}
+
+// device_calculateInfectionProbability, PandemicSim.cu:2307-2326
+__device__ __forceinline__ float infection_probability(const SimConst &c, int profile, int pday, int strain, int ksum)
+{
+    if (ksum == 0) ksum = 1;
+    float avg = __fmul_rn(c.shedding[profile][pday], c.infectiousness[strain]);
+    return __fdiv_rn(avg, __int2float_rn(ksum));
+}
+
+}  // namespace ptk

@@ -1,0 +1,109 @@
+// pt_kernels.h - kernel launchers and the device data model of the simulation.
+// Shared by the CUDA translation unit (pt_kernels.cu) and the host orchestration
+// (pt_sim.cpp); no CUDA-specific types beyond cudaStream_t appear here.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ptk {
+
+constexpr int kTypes = 14;
+constexpr int kMaxDays = 256;
+
+// Per-simulation constants, passed by value to every kernel (kernel-parameter
+// space is a uniform constant bank).
+struct SimConst {
+    int N, H, L;
+    int type_count[kTypes];
+    int type_offset[kTypes];
+    float shedding[6][10];
+    float infectiousness[2];
+    float pct_sympt;
+    uint64_t key0, key1;           // {(long)SEED[0], (long)SEED[1]}
+    uint64_t workplace_offset;     // W0: counter base of the workplace draws
+};
+
+// Device-resident scalars of one simulation.  The day loop reads and updates
+// these on the device, so a whole run needs no host round trip.
+struct Scalars {
+    unsigned long long rand_offset;     // next free Random123 counter
+    unsigned long long errand_offset;   // E0 of the current day's schedule
+    unsigned long long infect_offset;   // R0 of the current day's contacts
+    int infected;                       // infected count of the current day
+    int done;                           // set once a day counts zero infected
+    int days_run;                       // statistics rows written
+    int day;                            // current day index
+    int new_count;                      // entries in the new-infection list
+    int tile_ticket;                    // dynamic tile index of look-back kernels
+    int tile_ticket2;
+    int error;                          // nonzero: a bounded device wait gave up
+    int error_site;
+    int mid_count;                      // buckets for the warp sort
+    int big_count;                      // buckets for the block sort
+    int adults;
+    int pad[2];
+    int counts[kMaxDays][16];           // per-day status bins
+    int infected_per_day[kMaxDays];
+};
+
+// Device pointers of one simulation (all owned by one arena allocation).
+struct DevArrays {
+    uint32_t *state;          // N: status_p | status_s<<8 | day_p<<16 | day_s<<24
+    uint8_t *gen_p, *gen_s;   // N
+    uint8_t *age;             // N
+    int32_t *household;       // N
+    int32_t *hh_offset;       // H+1
+    int32_t *workplace;       // N
+    int32_t *wp_people;       // N
+    int32_t *wp_offset;       // L+1
+    int32_t *keys;            // 3N schedule keys
+    int32_t *bkt_offset;      // 10L+1
+    int32_t *bkt_count;       // 10L (histogram, then scatter cursor)
+    int32_t *bkt_people;      // 3N
+    int32_t *sort_tmp;        // 3N scratch for the large-bucket merge
+    int32_t *mid_list;        // 10L bucket ids for the warp sort
+    int32_t *big_list;        // 10L bucket ids for the block sort
+    int32_t *infected;        // N ascending infected ids
+    unsigned long long *claim;// 2N (victim, strain) -> min attempt key
+    int32_t *new_list;        // 2N first claims of the day
+    unsigned long long *tiles;// look-back tile status words
+    int tiles_cap;
+    Scalars *sc;
+};
+
+// Launch configuration helpers
+int sm_count();
+
+// ---- setup
+cudaError_t launch_household_types(const SimConst &c, uint8_t *types, int32_t *sizes, int *adults,
+                                   cudaStream_t s);
+cudaError_t launch_scan_exclusive(const int32_t *in, int32_t *out, int n, int clear_in,
+                                  unsigned long long *tiles, int *ticket, int *error,
+                                  const int *skip, cudaStream_t s);
+cudaError_t launch_generate_households(const SimConst &c, const uint8_t *types, const int32_t *hh_offset,
+                                       int32_t *household, uint8_t *age, cudaStream_t s);
+cudaError_t launch_assign_workplaces(const SimConst &c, uint8_t *age, int32_t *workplace, cudaStream_t s);
+cudaError_t launch_count_keys(const int32_t *keys, int n, int32_t *count, cudaStream_t s);
+cudaError_t launch_scatter_identity(const int32_t *keys, int n, const int32_t *offset, int32_t *cursor,
+                                    int32_t *out, cudaStream_t s);
+cudaError_t launch_sort_buckets(const int32_t *offset, int buckets, int32_t *people, int32_t *tmp,
+                                int32_t *mid_list, int32_t *big_list, Scalars *sc, const int *skip,
+                                cudaStream_t s);
+cudaError_t launch_init_status(int N, uint32_t *state, uint8_t *gen_p, uint8_t *gen_s,
+                               unsigned long long *claim, cudaStream_t s);
+cudaError_t launch_seed_infected(const int32_t *seeds, int P, int S, uint32_t *state, uint8_t *gen_p,
+                                 uint8_t *gen_s, cudaStream_t s);
+
+// ---- day
+cudaError_t launch_sweep(const SimConst &c, const DevArrays &d, int day, cudaStream_t s);
+cudaError_t launch_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
+cudaError_t launch_scatter_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
+cudaError_t launch_infect(const SimConst &c, const DevArrays &d, bool weekend, int day, cudaStream_t s);
+cudaError_t launch_apply(const DevArrays &d, int day, cudaStream_t s);
+
+// ---- final
+cudaError_t launch_gen_hist(const uint8_t *gen_p, const uint8_t *gen_s, int N, int *hist512, cudaStream_t s);
+
+uint64_t launches();
+
+}  // namespace ptk
