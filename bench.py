@@ -1,0 +1,377 @@
+#!/usr/bin/env python3
+"""Benchmark: simulated person-days per second of the GB300-native daily step.
+
+Workload (one GPU): 50,000,000 persons x 100 days, the reference's generator at
+people_scaling 21.24044 (21.24M households) and location_scaling 212.4044 (2.72M
+locations), R 1.5 / 1.2, 100 + 100 seed infections, seed 777.  Synthetic: the
+population is generated by the simulation itself from its seed, as in the reference.
+
+A step is one whole epidemic on the resident population: reset of the status arrays
+and initial infected, then the 100-day loop on the device.  value =
+persons x days simulated x steps / device time of the timed steps (CUDA events on
+the simulation's stream).  The per-person state (~4 GB) is far larger than the
+129 MB L2, so no flush is needed between steps.
+
+e2e: the same metric through the C ABI from host buffers: pt_create -> pt_setup
+(population generation) -> pt_run -> pt_final_gen_counts -> pt_destroy per step.
+
+--impl reference times the reference's algorithm on the host cores: the CPU
+restatement in oracle/ (the reference's own host code covers only schedule
+regeneration, so it cannot run a day), one simulated day of the same 50M workload
+per step, on every host thread for the per-person stages.
+
+Multi-GPU: replicas only (one independent simulation per rank, seed 777 + rank).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "plain_50M_persons_100_days"
+PARAMS = dict(max_days=100, r_pandemic=1.5, r_seasonal=1.2, initial_pandemic=100, initial_seasonal=100,
+              people_scaling=21.24044, location_scaling=212.4044, percent_symptomatic=1.0, asymp_factor=0.0)
+SEED = 777
+METRIC = "person-days/s on 1 GB300 (plain vs batched); surrogate scenarios/s at ≤5% error"
+UNIT = "person-days/s"
+FALLBACK_HBM_GBS = 6800.0
+
+# Algorithmic bytes per launch of each stage (layout-neutral compulsory traffic,
+# fields at their information size: status/day/gen/age 1 B, ids and offsets 4 B).
+#   sweep     4N read (status + day, both strains) + 4I written (infected list)
+#   schedule  weekday: 1N age read + 2 keys x 4 B written; weekend: 3 keys x 4 B
+#   scan      4B read + 4(B+1) written, B = 2L weekday / 10L weekend buckets
+#   scatter   4E keys read + 4E ids written, E = 2N / 3N entries
+#   sort      4E read + 4E written
+#   infect    79 B per infected weekday, 52 B weekend
+#   apply     claim 8 B read + 8 B reset + state 4 B + generation 1 B per new infection
+def stage_bytes(stage, weekend, N, L, I_mean, new_mean=0.0):
+    E = (3 if weekend else 2) * N
+    B = (10 if weekend else 2) * L
+    return {
+        "sweep": 4 * N + 4 * I_mean,
+        "schedule": (12 * N) if weekend else (9 * N),
+        "bucket_scan": 8 * B,
+        "bucket_scatter": 8 * E,
+        "bucket_sort": 8 * E,
+        "infect": (52 if weekend else 79) * I_mean,
+        "apply": 21 * new_mean,
+    }[stage]
+
+
+def day_bytes(weekend, N, L, I):
+    """Whole-day algorithmic bytes: 13N + 8L + 83I weekday, 16N + 40L + 56I weekend."""
+    return (16 * N + 40 * L + 56 * I) if weekend else (13 * N + 8 * L + 83 * I)
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the profiled kernel, from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    out = {}
+    try:
+        for line in open(path):
+            if line.startswith("traffic "):
+                kv = dict(x.split("=", 1) for x in line.split()[1:])
+                out[kv["stage"]] = float(kv["bytes_per_launch"])
+    except Exception:
+        pass
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=10)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_sample(days, threads, params=PARAMS, seed=SEED):
+    """The oracle on the same 50M workload: setup (untimed), then `days` simulated days."""
+    from oracle import build_oracle
+    from oracle.oracle import Oracle
+    build_oracle.build()
+    o = Oracle(params, seed, threads=threads)
+    o.setup()
+    N = o.view()["N"]
+    t0 = time.perf_counter()
+    ran = 0
+    for _ in range(days):
+        rc, _, _ = o.step_day()
+        if rc != 0:
+            break
+        ran += 1
+    dt = time.perf_counter() - t0
+    o.close()
+    return N, ran, dt
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    from oracle import build_oracle
+    from oracle.oracle import Oracle
+    build_oracle.build()
+    o = Oracle(PARAMS, SEED, threads=threads)
+    o.setup()
+    N = o.view()["N"]
+    for _ in range(args.warmup):
+        o.step_day()
+    t0 = time.perf_counter()
+    ran = 0
+    for _ in range(args.steps):
+        rc, _, _ = o.step_day()
+        if rc == 0:
+            ran += 1
+    dt = time.perf_counter() - t0
+    o.close()
+    value = N * ran / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32/f32",
+        "data": "synthetic (the reference's generator, seed 777)",
+        "config": {"workload": WORKLOAD, "persons": N, "days_per_step": 1, "parallelism": "host threads",
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d persons, days %d-%d after %d warm-up days, setup excluded" %
+                                   (N, args.warmup, args.warmup + args.steps - 1, args.warmup)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-days", type=int, default=7)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="population scale (profiling captures only; the bench line is for 1.0)")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import pandemicthrust_gb300 as pt
+    pt.build()
+    stream = torch.cuda.Stream()
+    seed = SEED + rank
+    params = dict(PARAMS)
+    params["people_scaling"] = PARAMS["people_scaling"] * args.scale
+    params["location_scaling"] = PARAMS["location_scaling"] * args.scale
+    sim = pt.PandemicSim(params, seed, stream=ctypes.c_void_p(stream.cuda_stream))
+    sim.setupSim()
+    info = sim.info()
+    N, L = info["number_people"], info["number_workplaces"]
+
+    # warm-up steps (untimed)
+    for _ in range(args.warmup):
+        sim.reset_epidemic()
+        sim.runToCompletion()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    sampler = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    launches0 = pt.launch_count()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    days_total = 0
+    for _ in range(args.steps):
+        sim.reset_epidemic()
+        counts, infected = sim.runToCompletion()
+        days_total += len(infected)
+    end.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    launches = pt.launch_count() - launches0
+    ms = start.elapsed_time(end)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        pd = torch.tensor([float(N) * days_total], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(pd)
+        person_days = float(pd.item())
+    else:
+        person_days = float(N) * days_total
+    value = person_days / (ms / 1000.0)
+
+    # stage breakdown: one more step with per-stage CUDA events (outside the timed region)
+    sim.set_timing(True)
+    sim.reset_epidemic()
+    counts, infected = sim.runToCompletion()
+    stages, (nwd, nwe) = sim.stage_ms()
+    sim.set_timing(False)
+    days = len(infected)
+    I_wd = [int(infected[d]) for d in range(days) if d % 7 < 5]
+    I_we = [int(infected[d]) for d in range(days) if d % 7 >= 5]
+    Imean_wd = sum(I_wd) / max(len(I_wd), 1)
+    Imean_we = sum(I_we) / max(len(I_we), 1)
+    # new infections of day d: drop of the susceptible bins (index 1 and 9) to day d+1
+    new = [int(counts[d][1] - counts[d + 1][1] + counts[d][9] - counts[d + 1][9]) for d in range(days - 1)] + [0]
+    new_wd = sum(new[d] for d in range(days) if d % 7 < 5) / max(len(I_wd), 1)
+    new_we = sum(new[d] for d in range(days) if d % 7 >= 5) / max(len(I_we), 1)
+    run_ms = sum(stages["weekday"].values()) + sum(stages["weekend"].values())
+    breakdown = {}
+    for name in pt.PandemicSim.STAGES:
+        tot = stages["weekday"][name] + stages["weekend"][name]
+        byt = (stage_bytes(name, False, N, L, Imean_wd, new_wd) * nwd +
+               stage_bytes(name, True, N, L, Imean_we, new_we) * nwe)
+        breakdown[name] = {"ms": round(tot, 3), "share": round(tot / run_ms, 4) if run_ms else None,
+                           "GBps": round(byt / (tot / 1000.0) / 1e9, 1) if tot > 0 else None}
+    dominant = max(pt.PandemicSim.STAGES, key=lambda n: stages["weekday"][n] + stages["weekend"][n])
+    dom_ms = stages["weekday"][dominant] + stages["weekend"][dominant]
+    dom_launches = nwd + nwe
+    dom_bytes = (stage_bytes(dominant, False, N, L, Imean_wd, new_wd) * nwd +
+                 stage_bytes(dominant, True, N, L, Imean_we, new_we) * nwe) / max(dom_launches, 1)
+    achieved = dom_bytes / (dom_ms / dom_launches / 1000.0) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = ncu_traffic().get(dominant)
+    all_bytes = sum(day_bytes(d % 7 >= 5, N, L, int(infected[d])) for d in range(days))
+    day_achieved = all_bytes / (run_ms / 1000.0) / 1e9
+
+    # e2e: whole pipeline through the C ABI from host buffers
+    e2e_value = None
+    h2d = d2h = 0
+    if args.e2e_steps > 0:
+        sim.close()
+        e2e_days = 0
+        e2e_start = torch.cuda.Event(enable_timing=True)
+        e2e_end = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e2e_start.record(stream)
+        for _ in range(args.e2e_steps):
+            s2 = pt.PandemicSim(params, seed, stream=ctypes.c_void_p(stream.cuda_stream))
+            s2.setupSim()
+            c2, i2 = s2.runToCompletion()
+            s2.final_gen_counts()
+            e2e_days += len(i2)
+            a, b = s2.transfer_bytes()
+            h2d += a
+            d2h += b
+            s2.close()
+        e2e_end.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = e2e_start.elapsed_time(e2e_end)
+        e2e_value = N * e2e_days / (e2e_ms / 1000.0) * (world if world > 1 else 1)
+        h2d //= args.e2e_steps
+        d2h //= args.e2e_steps
+    else:
+        sim.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        cN, cdays, cdt = cpu_sample(args.cpu_days, threads)
+        cpu = {"value": cN * cdays / cdt, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "oracle (C restatement) on the same %d-person workload, days 0-%d (setup excluded), "
+                         "%d host threads" % (cN, cdays - 1, threads)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8/i32/f32",
+            "data": "synthetic (the reference's population generator, seed 777 + rank)",
+            "config": {"workload": WORKLOAD, "persons": N, "households": info["number_households"],
+                       "locations": L, "days_per_step": days_total / args.steps,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (about 4 GB of per-person state)"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic},
+            "day_roofline": {"achieved": day_achieved, "peak": peak, "unit": "GB/s", "frac": day_achieved / peak,
+                             "bytes_per_run": all_bytes},
+            "stages": breakdown,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -130,14 +130,21 @@ pt_status pt_get_population(pt_sim *sim, int32_t *household, int32_t *household_
 pt_status pt_get_day_tables(pt_sim *sim, int32_t *infected, int32_t *keys, int32_t *people,
                             int32_t *offsets, int *entries, int *buckets);
 
-/* Milliseconds of device time per stage accumulated since the last call (CUDA
- * events on the simulation's stream; enabled by pt_set_timing).  Stages:
- * 0 sweep, 1 schedule, 2 bucket build, 3 infection, 4 apply. */
+/* Device time per stage, from CUDA events recorded on the simulation's stream
+ * around each stage of every day run while timing is enabled (pt_set_timing).
+ * ms[0..6] sum the weekday stages, ms[8..14] the weekend stages, in the order:
+ * sweep, schedule, bucket scan, bucket scatter, bucket sort, infection, apply.
+ * days[0], days[1] receive the number of weekdays and weekend days timed.  The sums
+ * reset after each call.  With timing enabled, a day run by pt_step_day or pt_run
+ * records events but adds no host synchronisation. */
 pt_status pt_set_timing(pt_sim *sim, int enabled);
-pt_status pt_get_stage_ms(pt_sim *sim, float ms[8]);
+pt_status pt_get_stage_ms(pt_sim *sim, float ms[16], int days[2]);
 
 /* Kernel launches issued by this library in the calling process so far. */
 uint64_t pt_launch_count(void);
+
+/* Bytes this simulation has copied host-to-device and device-to-host so far. */
+pt_status pt_transfer_bytes(const pt_sim *sim, uint64_t *h2d, uint64_t *d2h);
 
 void pt_destroy(pt_sim *sim);
 

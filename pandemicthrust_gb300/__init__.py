@@ -71,7 +71,7 @@ EXPORTS = [
     "pt_params_from_csv", "pt_seed_from_file", "pt_create", "pt_setup", "pt_step_day", "pt_run",
     "pt_final_gen_counts", "pt_reset_epidemic", "pt_get_info", "pt_get_person_state",
     "pt_get_population", "pt_get_day_tables", "pt_set_timing", "pt_get_stage_ms",
-    "pt_launch_count", "pt_destroy", "pt_last_error",
+    "pt_launch_count", "pt_transfer_bytes", "pt_destroy", "pt_last_error",
 ]
 
 _lib = None
@@ -105,9 +105,10 @@ def load_library(path=None):
     lib.pt_get_population.argtypes = [vp] + [i32p] * 5
     lib.pt_get_day_tables.argtypes = [vp, i32p, i32p, i32p, i32p, ip, ip]
     lib.pt_set_timing.argtypes = [vp, ctypes.c_int]
-    lib.pt_get_stage_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
+    lib.pt_get_stage_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ip]
     lib.pt_launch_count.restype = ctypes.c_uint64
     lib.pt_launch_count.argtypes = []
+    lib.pt_transfer_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
     lib.pt_destroy.argtypes = [vp]
     lib.pt_last_error.argtypes = [vp]
     lib.pt_last_error.restype = ctypes.c_char_p
@@ -210,10 +211,22 @@ class PandemicSim:
     def set_timing(self, on=True):
         self._check(self.lib.pt_set_timing(self.h, 1 if on else 0))
 
+    STAGES = ("sweep", "schedule", "bucket_scan", "bucket_scatter", "bucket_sort", "infect", "apply")
+
     def stage_ms(self):
-        a = (ctypes.c_float * 8)()
-        self._check(self.lib.pt_get_stage_ms(self.h, a))
-        return list(a)
+        """Device ms per stage since the last call: ({weekday: {...}, weekend: {...}}, (weekdays, weekend days))."""
+        a = (ctypes.c_float * 16)()
+        days = (ctypes.c_int * 2)()
+        self._check(self.lib.pt_get_stage_ms(self.h, a, days))
+        out = {"weekday": {n: a[k] for k, n in enumerate(self.STAGES)},
+               "weekend": {n: a[8 + k] for k, n in enumerate(self.STAGES)}}
+        return out, (days[0], days[1])
+
+    def transfer_bytes(self):
+        """(host-to-device, device-to-host) bytes this simulation has copied."""
+        a, b = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        self._check(self.lib.pt_transfer_bytes(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def close(self):
         if getattr(self, "h", None):

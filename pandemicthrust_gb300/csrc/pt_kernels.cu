@@ -792,8 +792,11 @@ cudaError_t launch_schedule(const SimConst &c, const DevArrays &d, bool weekend,
         k_sched_weekday<<<std::max(1, blocks), 256, 0, s>>>(c, d.age, d.keys, d.bkt_count, d.sc);
     }
     count_launch();
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s)
+{
     const int B = (weekend ? 10 : 2) * c.L;
     LookBack lb = make_lb(d.tiles, d.tiles_cap, &d.sc->error);
     int blocks = std::max(1, div_up(B, kScanTile));
@@ -822,8 +825,11 @@ cudaError_t launch_scatter_schedule(const SimConst &c, const DevArrays &d, bool 
     k_scatter_sched<<<std::max(1, blocks), 256, 0, s>>>(d.keys, c.N, weekend ? 1 : 0, d.bkt_offset, d.bkt_count,
                                                         d.bkt_people, d.sc);
     count_launch();
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sort_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s)
+{
     const int B = (weekend ? 10 : 2) * c.L;
     return launch_sort_buckets(d.bkt_offset, B, d.bkt_people, d.sort_tmp, d.mid_list, d.big_list, d.sc,
                                &d.sc->done, s);

@@ -97,7 +97,9 @@ cudaError_t launch_seed_infected(const int32_t *seeds, int P, int S, uint32_t *s
 // ---- day
 cudaError_t launch_sweep(const SimConst &c, const DevArrays &d, int day, cudaStream_t s);
 cudaError_t launch_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
+cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
 cudaError_t launch_scatter_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
+cudaError_t launch_sort_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
 cudaError_t launch_infect(const SimConst &c, const DevArrays &d, bool weekend, int day, cudaStream_t s);
 cudaError_t launch_apply(const DevArrays &d, int day, cudaStream_t s);
 

@@ -59,14 +59,34 @@ struct pt_sim {
     int days_run = 0;
     std::string err;
     bool timing = false;
-    cudaEvent_t ev[12] = {};
-    float stage_ms[8] = {0};
+    std::vector<cudaEvent_t> day_events;  // kMaxDays x (stages + 1), created on demand
+    std::vector<int> timed_days;
+    float stage_ms[16] = {0};             // [weekday stages 0..7, weekend stages 8..15]
+    int stage_days[2] = {0, 0};
     // per-day results mirrored on the host
     std::vector<int> counts;        // kMaxDays * 16
     std::vector<int> infected;      // kMaxDays
     float max_prop = 0.f;
     int max_prop_day = 0;
+    mutable uint64_t h2d_bytes = 0, d2h_bytes = 0;  // host<->device copies issued
 };
+
+// Every host<->device copy of the library goes through these, so the bytes a call
+// moves across PCIe/C2C can be reported (pt_transfer_bytes).
+static cudaError_t pt_memcpy(const pt_sim *s, void *dst, const void *src, size_t n, cudaMemcpyKind k,
+                             cudaStream_t st)
+{
+    if (k == cudaMemcpyHostToDevice) s->h2d_bytes += n;
+    else if (k == cudaMemcpyDeviceToHost) s->d2h_bytes += n;
+    return cudaMemcpyAsync(dst, src, n, k, st);
+}
+
+static cudaError_t pt_memcpy_sync(const pt_sim *s, void *dst, const void *src, size_t n, cudaMemcpyKind k)
+{
+    cudaError_t e = pt_memcpy(s, dst, src, n, k, s->stream);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s->stream);
+}
 
 static pt_status fail(pt_sim *s, pt_status st, const std::string &msg)
 {
@@ -131,7 +151,7 @@ static pt_status reset_epidemic(pt_sim *s)
     CK(ptk::launch_init_status(N, d.state, d.gen_p, d.gen_s, d.claim, s->stream), "init_status");
     const int P = s->params.initial_pandemic, S = s->params.initial_seasonal;
     if (P + S > 0) {
-        CK(cudaMemcpyAsync(s->d_seeds, s->seed_list.data(), sizeof(int32_t) * (P + S), cudaMemcpyHostToDevice,
+        CK(pt_memcpy(s, s->d_seeds, s->seed_list.data(), sizeof(int32_t) * (P + S), cudaMemcpyHostToDevice,
                            s->stream), "seed copy");
         CK(ptk::launch_seed_infected(s->d_seeds, P, S, d.state, d.gen_p, d.gen_s, s->stream), "seed");
     }
@@ -140,7 +160,7 @@ static pt_status reset_epidemic(pt_sim *s)
     // rand_offset after setup: H/4 (household types) + N/4 (workplaces)
     z.rand_offset = (unsigned long long)(s->c.H / 4) + (unsigned long long)(N / 4);
     z.adults = s->adults;
-    CK(cudaMemcpyAsync(d.sc, &z, sizeof(z), cudaMemcpyHostToDevice, s->stream), "scalars");
+    CK(pt_memcpy(s, d.sc, &z, sizeof(z), cudaMemcpyHostToDevice, s->stream), "scalars");
     CK(cudaStreamSynchronize(s->stream), "reset sync");
     s->day = 0;
     s->stopped = false;
@@ -160,8 +180,6 @@ pt_status pt_setup(pt_sim *s)
         CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         s->own_stream = true;
     }
-    if (!s->ev[0])
-        for (auto &e : s->ev) CK(cudaEventCreate(&e), "cudaEventCreate");
     ptk::SimConst &c = s->c;
     const int H = c.H, L = c.L;
     const long long maxN = 5ll * H;  // the largest household type holds 5 persons
@@ -195,8 +213,8 @@ pt_status pt_setup(pt_sim *s)
     CK(ptk::launch_scan_exclusive(sizes, d.hh_offset, H, 0, d.tiles, ctl, &d.sc->error, nullptr, s->stream),
        "household scan");
     int hN = 0, hA = 0;
-    CK(cudaMemcpyAsync(&hN, d.hh_offset + H, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "N copy");
-    CK(cudaMemcpyAsync(&hA, &d.sc->adults, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "adults copy");
+    CK(pt_memcpy(s, &hN, d.hh_offset + H, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "N copy");
+    CK(pt_memcpy(s, &hA, &d.sc->adults, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "adults copy");
     CK(cudaStreamSynchronize(s->stream), "setup sync");
     if (hN <= 0) return fail(s, PT_ERR_STATE, "population is empty");
     const int N = hN;
@@ -257,7 +275,7 @@ pt_status pt_setup(pt_sim *s)
     // initial infected: rand() % N draws continue the seed sequence (PandemicSim.cu:708-758)
     s->seed_list = pth::unique_numbers(*s->rng, P + S, N);
     int derr = 0;
-    CK(cudaMemcpyAsync(&derr, &d.sc->error, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "error flag");
+    CK(pt_memcpy(s, &derr, &d.sc->error, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "error flag");
     CK(cudaStreamSynchronize(s->stream), "setup sync");
     cudaFree(s->setup_mem);
     s->setup_mem = nullptr;
@@ -275,42 +293,63 @@ pt_status pt_reset_epidemic(pt_sim *s)
     return reset_epidemic(s);
 }
 
-// Enqueues one day: sweep, schedule + bucket build, infection, apply.  All kernels
-// after the sweep skip themselves on the device when the day counted no infected.
+// Stage boundaries recorded per day when timing is on.
+enum { kStSweep, kStSchedule, kStScan, kStScatter, kStSort, kStInfect, kStApply, kStages };
+
+static cudaEvent_t stage_event(pt_sim *s, int day, int k)
+{
+    return s->day_events[(size_t)day * (kStages + 1) + k];
+}
+
+// Enqueues one day: sweep, schedule, bucket build (scan, scatter, sort), infection,
+// apply.  Every kernel after the sweep skips itself on the device when the day
+// counted no infected.
 static pt_status enqueue_day(pt_sim *s, int day)
 {
     const bool weekend = (day % 7) >= 5;  // PandemicSim.h:283-284
     const ptk::SimConst &c = s->c;
     const ptk::DevArrays &d = s->d;
     cudaStream_t st = s->stream;
-    if (s->timing) cudaEventRecord(s->ev[0], st);
+    const bool t = s->timing;
+    if (t) cudaEventRecord(stage_event(s, day, 0), st);
     CK(ptk::launch_sweep(c, d, day, st), "sweep");
-    if (s->timing) cudaEventRecord(s->ev[1], st);
+    if (t) cudaEventRecord(stage_event(s, day, 1), st);
     CK(ptk::launch_schedule(c, d, weekend, st), "schedule");
-    if (s->timing) cudaEventRecord(s->ev[2], st);
-    CK(ptk::launch_scatter_schedule(c, d, weekend, st), "bucket build");
-    if (s->timing) cudaEventRecord(s->ev[3], st);
+    if (t) cudaEventRecord(stage_event(s, day, 2), st);
+    CK(ptk::launch_bucket_scan(c, d, weekend, st), "bucket scan");
+    if (t) cudaEventRecord(stage_event(s, day, 3), st);
+    CK(ptk::launch_scatter_schedule(c, d, weekend, st), "bucket scatter");
+    if (t) cudaEventRecord(stage_event(s, day, 4), st);
+    CK(ptk::launch_sort_schedule(c, d, weekend, st), "bucket sort");
+    if (t) cudaEventRecord(stage_event(s, day, 5), st);
     CK(ptk::launch_infect(c, d, weekend, day, st), "infect");
-    if (s->timing) cudaEventRecord(s->ev[4], st);
+    if (t) cudaEventRecord(stage_event(s, day, 6), st);
     CK(ptk::launch_apply(d, day, st), "apply");
-    if (s->timing) cudaEventRecord(s->ev[5], st);
+    if (t) cudaEventRecord(stage_event(s, day, 7), st);
+    if (t) s->timed_days.push_back(day);
     return PT_OK;
 }
 
 static void accumulate_timing(pt_sim *s)
 {
     if (!s->timing) return;
-    cudaEventSynchronize(s->ev[5]);
-    for (int k = 0; k < 5; k++) {
-        float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, s->ev[k], s->ev[k + 1]) == cudaSuccess) s->stage_ms[k] += ms;
+    cudaStreamSynchronize(s->stream);
+    for (int day : s->timed_days) {
+        const bool weekend = (day % 7) >= 5;
+        for (int k = 0; k < kStages; k++) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, stage_event(s, day, k), stage_event(s, day, k + 1)) == cudaSuccess)
+                s->stage_ms[(weekend ? 8 : 0) + k] += ms;
+        }
+        s->stage_days[weekend ? 1 : 0]++;
     }
+    s->timed_days.clear();
 }
 
 static pt_status check_device_error(pt_sim *s)
 {
     int e = 0;
-    CK(cudaMemcpyAsync(&e, &s->d.sc->error, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "error flag");
+    CK(pt_memcpy(s, &e, &s->d.sc->error, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "error flag");
     CK(cudaStreamSynchronize(s->stream), "sync");
     if (e) return fail(s, PT_ERR_TIMEOUT, "a device-side wait gave up (look-back ordering)");
     return PT_OK;
@@ -336,8 +375,8 @@ pt_status pt_step_day(pt_sim *s, int counts16[16], int *infected_count)
     pt_status st = enqueue_day(s, day);
     if (st != PT_OK) return st;
     int buf[17];
-    CK(cudaMemcpyAsync(buf, s->d.sc->counts[day], 16 * sizeof(int), cudaMemcpyDeviceToHost, s->stream), "counts");
-    CK(cudaMemcpyAsync(buf + 16, &s->d.sc->infected_per_day[day], sizeof(int), cudaMemcpyDeviceToHost, s->stream),
+    CK(pt_memcpy(s, buf, s->d.sc->counts[day], 16 * sizeof(int), cudaMemcpyDeviceToHost, s->stream), "counts");
+    CK(pt_memcpy(s, buf + 16, &s->d.sc->infected_per_day[day], sizeof(int), cudaMemcpyDeviceToHost, s->stream),
        "infected");
     st = check_device_error(s);
     if (st != PT_OK) return st;
@@ -370,13 +409,14 @@ pt_status pt_run(pt_sim *s, int *counts, int *infected, int *days_run)
     // one copy of all per-day results
     std::vector<int> hc(ptk::kMaxDays * 16), hi(ptk::kMaxDays);
     int rows = 0;
-    CK(cudaMemcpyAsync(hc.data(), s->d.sc->counts, hc.size() * sizeof(int), cudaMemcpyDeviceToHost, s->stream),
+    CK(pt_memcpy(s, hc.data(), s->d.sc->counts, hc.size() * sizeof(int), cudaMemcpyDeviceToHost, s->stream),
        "counts");
-    CK(cudaMemcpyAsync(hi.data(), s->d.sc->infected_per_day, hi.size() * sizeof(int), cudaMemcpyDeviceToHost,
+    CK(pt_memcpy(s, hi.data(), s->d.sc->infected_per_day, hi.size() * sizeof(int), cudaMemcpyDeviceToHost,
                        s->stream), "infected");
-    CK(cudaMemcpyAsync(&rows, &s->d.sc->days_run, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "rows");
+    CK(pt_memcpy(s, &rows, &s->d.sc->days_run, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "rows");
     pt_status st = check_device_error(s);
     if (st != PT_OK) return st;
+    accumulate_timing(s);
     if (!s->stopped) {
         for (int day = first; day < rows; day++) {
             std::memcpy(&s->counts[day * 16], &hc[day * 16], 16 * sizeof(int));
@@ -402,7 +442,7 @@ pt_status pt_final_gen_counts(pt_sim *s, int gen_p[256], int gen_s[256])
     if (!s->setup_done) return fail(s, PT_ERR_STATE, "pt_final_gen_counts before pt_setup");
     CK(ptk::launch_gen_hist(s->d.gen_p, s->d.gen_s, s->c.N, s->d_hist, s->stream), "gen hist");
     int h[512];
-    CK(cudaMemcpyAsync(h, s->d_hist, sizeof(h), cudaMemcpyDeviceToHost, s->stream), "hist copy");
+    CK(pt_memcpy(s, h, s->d_hist, sizeof(h), cudaMemcpyDeviceToHost, s->stream), "hist copy");
     CK(cudaStreamSynchronize(s->stream), "sync");
     std::memcpy(gen_p, h, 256 * sizeof(int));
     std::memcpy(gen_s, h + 256, 256 * sizeof(int));
@@ -434,7 +474,7 @@ pt_status pt_get_info(const pt_sim *s, pt_info *out)
     out->device_bytes = s->arena_bytes + s->small_bytes;
     if (s->setup_done) {
         unsigned long long ro = 0;
-        cudaMemcpy(&ro, &s->d.sc->rand_offset, sizeof(ro), cudaMemcpyDeviceToHost);
+        pt_memcpy_sync(s, &ro, &s->d.sc->rand_offset, sizeof(ro), cudaMemcpyDeviceToHost);
         out->rand_offset = ro;
     }
     return PT_OK;
@@ -449,7 +489,7 @@ pt_status pt_get_person_state(pt_sim *s, uint8_t *status_p, uint8_t *status_s, u
     CK(cudaStreamSynchronize(s->stream), "sync");
     if (status_p || status_s || day_p || day_s) {
         std::vector<uint32_t> st(N);
-        CK(cudaMemcpy(st.data(), s->d.state, N * 4, cudaMemcpyDeviceToHost), "state copy");
+        CK(pt_memcpy_sync(s, st.data(), s->d.state, N * 4, cudaMemcpyDeviceToHost), "state copy");
         for (size_t i = 0; i < N; i++) {
             if (status_p) status_p[i] = (uint8_t)(st[i] & 0xFF);
             if (status_s) status_s[i] = (uint8_t)((st[i] >> 8) & 0xFF);
@@ -457,9 +497,9 @@ pt_status pt_get_person_state(pt_sim *s, uint8_t *status_p, uint8_t *status_s, u
             if (day_s) day_s[i] = (uint8_t)(st[i] >> 24);
         }
     }
-    if (gen_p) CK(cudaMemcpy(gen_p, s->d.gen_p, N, cudaMemcpyDeviceToHost), "gen copy");
-    if (gen_s) CK(cudaMemcpy(gen_s, s->d.gen_s, N, cudaMemcpyDeviceToHost), "gen copy");
-    if (age) CK(cudaMemcpy(age, s->d.age, N, cudaMemcpyDeviceToHost), "age copy");
+    if (gen_p) CK(pt_memcpy_sync(s, gen_p, s->d.gen_p, N, cudaMemcpyDeviceToHost), "gen copy");
+    if (gen_s) CK(pt_memcpy_sync(s, gen_s, s->d.gen_s, N, cudaMemcpyDeviceToHost), "gen copy");
+    if (age) CK(pt_memcpy_sync(s, age, s->d.age, N, cudaMemcpyDeviceToHost), "age copy");
     return PT_OK;
 }
 
@@ -470,13 +510,13 @@ pt_status pt_get_population(pt_sim *s, int32_t *household, int32_t *household_of
     if (!s->setup_done) return fail(s, PT_ERR_STATE, "population before pt_setup");
     const size_t N = (size_t)s->c.N;
     CK(cudaStreamSynchronize(s->stream), "sync");
-    if (household) CK(cudaMemcpy(household, s->d.household, N * 4, cudaMemcpyDeviceToHost), "copy");
+    if (household) CK(pt_memcpy_sync(s, household, s->d.household, N * 4, cudaMemcpyDeviceToHost), "copy");
     if (household_offset)
-        CK(cudaMemcpy(household_offset, s->d.hh_offset, ((size_t)s->c.H + 1) * 4, cudaMemcpyDeviceToHost), "copy");
-    if (workplace) CK(cudaMemcpy(workplace, s->d.workplace, N * 4, cudaMemcpyDeviceToHost), "copy");
-    if (workplace_people) CK(cudaMemcpy(workplace_people, s->d.wp_people, N * 4, cudaMemcpyDeviceToHost), "copy");
+        CK(pt_memcpy_sync(s, household_offset, s->d.hh_offset, ((size_t)s->c.H + 1) * 4, cudaMemcpyDeviceToHost), "copy");
+    if (workplace) CK(pt_memcpy_sync(s, workplace, s->d.workplace, N * 4, cudaMemcpyDeviceToHost), "copy");
+    if (workplace_people) CK(pt_memcpy_sync(s, workplace_people, s->d.wp_people, N * 4, cudaMemcpyDeviceToHost), "copy");
     if (workplace_offset)
-        CK(cudaMemcpy(workplace_offset, s->d.wp_offset, ((size_t)s->c.L + 1) * 4, cudaMemcpyDeviceToHost), "copy");
+        CK(pt_memcpy_sync(s, workplace_offset, s->d.wp_offset, ((size_t)s->c.L + 1) * 4, cudaMemcpyDeviceToHost), "copy");
     return PT_OK;
 }
 
@@ -487,37 +527,56 @@ pt_status pt_get_day_tables(pt_sim *s, int32_t *infected, int32_t *keys, int32_t
     if (!s->setup_done) return fail(s, PT_ERR_STATE, "tables before pt_setup");
     CK(cudaStreamSynchronize(s->stream), "sync");
     ptk::Scalars sc;
-    CK(cudaMemcpy(&sc, s->d.sc, sizeof(sc), cudaMemcpyDeviceToHost), "scalars");
+    CK(pt_memcpy_sync(s, &sc, s->d.sc, sizeof(sc), cudaMemcpyDeviceToHost), "scalars");
     const int day = sc.day;
     const bool weekend = (day % 7) >= 5;
     const int E = (weekend ? 3 : 2) * s->c.N, B = (weekend ? 10 : 2) * s->c.L;
     if (entries) *entries = E;
     if (buckets) *buckets = B;
     if (infected && sc.infected > 0)
-        CK(cudaMemcpy(infected, s->d.infected, (size_t)sc.infected * 4, cudaMemcpyDeviceToHost), "copy");
-    if (keys) CK(cudaMemcpy(keys, s->d.keys, (size_t)E * 4, cudaMemcpyDeviceToHost), "copy");
-    if (people) CK(cudaMemcpy(people, s->d.bkt_people, (size_t)E * 4, cudaMemcpyDeviceToHost), "copy");
-    if (offsets) CK(cudaMemcpy(offsets, s->d.bkt_offset, ((size_t)B + 1) * 4, cudaMemcpyDeviceToHost), "copy");
+        CK(pt_memcpy_sync(s, infected, s->d.infected, (size_t)sc.infected * 4, cudaMemcpyDeviceToHost), "copy");
+    if (keys) CK(pt_memcpy_sync(s, keys, s->d.keys, (size_t)E * 4, cudaMemcpyDeviceToHost), "copy");
+    if (people) CK(pt_memcpy_sync(s, people, s->d.bkt_people, (size_t)E * 4, cudaMemcpyDeviceToHost), "copy");
+    if (offsets) CK(pt_memcpy_sync(s, offsets, s->d.bkt_offset, ((size_t)B + 1) * 4, cudaMemcpyDeviceToHost), "copy");
     return PT_OK;
 }
 
 pt_status pt_set_timing(pt_sim *s, int enabled)
 {
     if (!s) return PT_ERR_ARG;
+    if (enabled && s->day_events.empty()) {
+        s->day_events.resize((size_t)ptk::kMaxDays * (kStages + 1));
+        for (auto &e : s->day_events) CK(cudaEventCreate(&e), "cudaEventCreate");
+    }
     s->timing = enabled != 0;
     std::memset(s->stage_ms, 0, sizeof(s->stage_ms));
+    s->stage_days[0] = s->stage_days[1] = 0;
     return PT_OK;
 }
 
-pt_status pt_get_stage_ms(pt_sim *s, float ms[8])
+pt_status pt_get_stage_ms(pt_sim *s, float ms[16], int days[2])
 {
     if (!s || !ms) return PT_ERR_ARG;
+    accumulate_timing(s);
     std::memcpy(ms, s->stage_ms, sizeof(s->stage_ms));
+    if (days) {
+        days[0] = s->stage_days[0];
+        days[1] = s->stage_days[1];
+    }
     std::memset(s->stage_ms, 0, sizeof(s->stage_ms));
+    s->stage_days[0] = s->stage_days[1] = 0;
     return PT_OK;
 }
 
 uint64_t pt_launch_count(void) { return ptk::launches(); }
+
+pt_status pt_transfer_bytes(const pt_sim *s, uint64_t *h2d, uint64_t *d2h)
+{
+    if (!s) return PT_ERR_ARG;
+    if (h2d) *h2d = s->h2d_bytes;
+    if (d2h) *d2h = s->d2h_bytes;
+    return PT_OK;
+}
 
 void pt_destroy(pt_sim *s)
 {
@@ -526,7 +585,7 @@ void pt_destroy(pt_sim *s)
     cudaFree(s->arena_mem);
     cudaFree(s->setup_mem);
     cudaFree(s->small_mem);
-    for (auto &e : s->ev)
+    for (auto &e : s->day_events)
         if (e) cudaEventDestroy(e);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
