@@ -25,6 +25,7 @@ namespace ptk {
 
 static std::atomic<uint64_t> g_launches{0};
 uint64_t launches() { return g_launches.load(); }
+void add_launches(int64_t n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
 static inline void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 int sm_count()

@@ -107,5 +107,6 @@ cudaError_t launch_apply(const DevArrays &d, int day, cudaStream_t s);
 cudaError_t launch_gen_hist(const uint8_t *gen_p, const uint8_t *gen_s, int N, int *hist512, cudaStream_t s);
 
 uint64_t launches();
+void add_launches(int64_t n);  // kernels run by a replayed graph
 
 }  // namespace ptk

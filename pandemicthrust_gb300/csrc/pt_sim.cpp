@@ -69,6 +69,11 @@ struct pt_sim {
     float max_prop = 0.f;
     int max_prop_day = 0;
     mutable uint64_t h2d_bytes = 0, d2h_bytes = 0;  // host<->device copies issued
+    // The whole day loop (days 0..max_days-1) captured once and replayed by pt_run.
+    // Every per-day decision (early stop, counters, offsets) reads device scalars,
+    // so the same graph serves every run after pt_reset_epidemic.
+    cudaGraphExec_t run_graph = nullptr;
+    uint64_t graph_kernels = 0;
 };
 
 // Every host<->device copy of the library goes through these, so the bytes a call
@@ -401,9 +406,32 @@ pt_status pt_run(pt_sim *s, int *counts, int *infected, int *days_run)
     if (!s->setup_done) return fail(s, PT_ERR_STATE, "pt_run before pt_setup");
     const int first = s->day, M = s->params.max_days;
     if (!s->stopped) {
-        for (int day = first; day < M; day++) {
-            pt_status st = enqueue_day(s, day);
-            if (st != PT_OK) return st;
+        if (first == 0 && !s->timing && M > 0) {
+            if (!s->run_graph) {
+                const uint64_t before = ptk::launches();
+                CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+                pt_status st = PT_OK;
+                for (int day = 0; day < M && st == PT_OK; day++) st = enqueue_day(s, day);
+                cudaGraph_t g = nullptr;
+                cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+                if (st != PT_OK) {
+                    if (g) cudaGraphDestroy(g);
+                    return st;
+                }
+                CK(e, "end capture");
+                e = cudaGraphInstantiate(&s->run_graph, g, 0);
+                cudaGraphDestroy(g);
+                CK(e, "graph instantiate");
+                s->graph_kernels = ptk::launches() - before;
+                ptk::add_launches(-(int64_t)s->graph_kernels);  // counted when the graph runs
+            }
+            CK(cudaGraphLaunch(s->run_graph, s->stream), "graph launch");
+            ptk::add_launches((int64_t)s->graph_kernels);
+        } else {
+            for (int day = first; day < M; day++) {
+                pt_status st = enqueue_day(s, day);
+                if (st != PT_OK) return st;
+            }
         }
     }
     // one copy of all per-day results
@@ -582,6 +610,7 @@ void pt_destroy(pt_sim *s)
 {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->run_graph) cudaGraphExecDestroy(s->run_graph);
     cudaFree(s->arena_mem);
     cudaFree(s->setup_mem);
     cudaFree(s->small_mem);
