@@ -44,21 +44,20 @@ FALLBACK_HBM_GBS = 6800.0
 
 # Algorithmic bytes per launch of each stage (layout-neutral compulsory traffic,
 # fields at their information size: status/day/gen/age 1 B, ids and offsets 4 B).
+# E = entries of the day's schedule (2N weekday, 3N weekend); Bc = buckets a day can
+# use (2 hours x locations of types 8-13 weekday, 10 hours x types 9-13 weekend).
 #   sweep     4N read (status + day, both strains) + 4I written (infected list)
-#   schedule  weekday: 1N age read + 2 keys x 4 B written; weekend: 3 keys x 4 B
-#   scan      4B read + 4(B+1) written, B = 2L weekday / 10L weekend buckets
-#   scatter   4E keys read + 4E ids written, E = 2N / 3N entries
-#   sort      4E read + 4E written
+#   schedule  weekday 1N age read + 4E keys written; weekend 4E keys written
+#   scan      4Bc counts read + 4(Bc+1) offsets written
+#   sort      4E schedule read + 4E bucket table written
 #   infect    79 B per infected weekday, 52 B weekend
 #   apply     claim 8 B read + 8 B reset + state 4 B + generation 1 B per new infection
-def stage_bytes(stage, weekend, N, L, I_mean, new_mean=0.0):
+def stage_bytes(stage, weekend, N, Bc, I_mean, new_mean=0.0):
     E = (3 if weekend else 2) * N
-    B = (10 if weekend else 2) * L
     return {
         "sweep": 4 * N + 4 * I_mean,
-        "schedule": (12 * N) if weekend else (9 * N),
-        "bucket_scan": 8 * B,
-        "bucket_scatter": 8 * E,
+        "schedule": (4 * E) if weekend else (N + 4 * E),
+        "bucket_scan": 8 * Bc,
         "bucket_sort": 8 * E,
         "infect": (52 if weekend else 79) * I_mean,
         "apply": 21 * new_mean,
@@ -236,6 +235,8 @@ def main():
     sim.setupSim()
     info = sim.info()
     N, L = info["number_people"], info["number_workplaces"]
+    Bc_wd = 2 * (L - info["type_offset"][8])
+    Bc_we = 10 * (L - info["type_offset"][9])
 
     # warm-up steps (untimed)
     for _ in range(args.warmup):
@@ -295,15 +296,15 @@ def main():
     breakdown = {}
     for name in pt.PandemicSim.STAGES:
         tot = stages["weekday"][name] + stages["weekend"][name]
-        byt = (stage_bytes(name, False, N, L, Imean_wd, new_wd) * nwd +
-               stage_bytes(name, True, N, L, Imean_we, new_we) * nwe)
+        byt = (stage_bytes(name, False, N, Bc_wd, Imean_wd, new_wd) * nwd +
+               stage_bytes(name, True, N, Bc_we, Imean_we, new_we) * nwe)
         breakdown[name] = {"ms": round(tot, 3), "share": round(tot / run_ms, 4) if run_ms else None,
                            "GBps": round(byt / (tot / 1000.0) / 1e9, 1) if tot > 0 else None}
     dominant = max(pt.PandemicSim.STAGES, key=lambda n: stages["weekday"][n] + stages["weekend"][n])
     dom_ms = stages["weekday"][dominant] + stages["weekend"][dominant]
     dom_launches = nwd + nwe
-    dom_bytes = (stage_bytes(dominant, False, N, L, Imean_wd, new_wd) * nwd +
-                 stage_bytes(dominant, True, N, L, Imean_we, new_we) * nwe) / max(dom_launches, 1)
+    dom_bytes = (stage_bytes(dominant, False, N, Bc_wd, Imean_wd, new_wd) * nwd +
+                 stage_bytes(dominant, True, N, Bc_we, Imean_we, new_we) * nwe) / max(dom_launches, 1)
     achieved = dom_bytes / (dom_ms / dom_launches / 1000.0) / 1e9
     peak, peak_kind = measured_peaks()
     traffic = ncu_traffic().get(dominant)

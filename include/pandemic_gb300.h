@@ -132,8 +132,8 @@ pt_status pt_get_day_tables(pt_sim *sim, int32_t *infected, int32_t *keys, int32
 
 /* Device time per stage, from CUDA events recorded on the simulation's stream
  * around each stage of every day run while timing is enabled (pt_set_timing).
- * ms[0..6] sum the weekday stages, ms[8..14] the weekend stages, in the order:
- * sweep, schedule, bucket scan, bucket scatter, bucket sort, infection, apply.
+ * ms[0..5] sum the weekday stages, ms[8..13] the weekend stages, in the order:
+ * sweep, schedule, bucket scan, bucket radix sort, infection, apply.
  * days[0], days[1] receive the number of weekdays and weekend days timed.  The sums
  * reset after each call.  With timing enabled, a day run by pt_step_day or pt_run
  * records events but adds no host synchronisation. */

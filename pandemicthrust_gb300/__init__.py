@@ -211,7 +211,7 @@ class PandemicSim:
     def set_timing(self, on=True):
         self._check(self.lib.pt_set_timing(self.h, 1 if on else 0))
 
-    STAGES = ("sweep", "schedule", "bucket_scan", "bucket_scatter", "bucket_sort", "infect", "apply")
+    STAGES = ("sweep", "schedule", "bucket_scan", "bucket_sort", "infect", "apply")
 
     def stage_ms(self):
         """Device ms per stage since the last call: ({weekday: {...}, weekend: {...}}, (weekdays, weekend days))."""

@@ -219,8 +219,12 @@ __device__ __forceinline__ int fish_weekend_dest(const SimConst &c, uint32_t r)
 }
 
 // device_generateWeekendErrands, PandemicSim.cu:980-1014: three distinct hours of
-// ten, each with a destination; key = destination + hour * L.
-__device__ __forceinline__ void weekend_errands(const SimConst &c, const TfKey &k, uint64_t ctr, int out[3])
+// ten, each with a destination.  The reference's key is destination + hour * L;
+// weekend destinations all lie in [lo, L) (lo = first location of type 9), so the
+// bucket index used here is the order-preserving compact form hour * R + dest - lo,
+// R = L - lo.
+__device__ __forceinline__ void weekend_errands(const SimConst &c, const TfKey &k, uint64_t ctr, int lo, int R,
+                                                int out[3])
 {
     uint32_t w[8];
     tf2x64(k, ctr, w);
@@ -230,9 +234,9 @@ __device__ __forceinline__ void weekend_errands(const SimConst &c, const TfKey &
     if (h2 == h1) h2 = (h2 + 1) % 10;
     int h3 = (int)(w[2] % 10u);
     while (h3 == h1 || h3 == h2) h3 = (h3 + 1) % 10;
-    out[0] = fish_weekend_dest(c, w[3]) + h1 * c.L;
-    out[1] = fish_weekend_dest(c, w[4]) + h2 * c.L;
-    out[2] = fish_weekend_dest(c, w[5]) + h3 * c.L;
+    out[0] = fish_weekend_dest(c, w[3]) - lo + h1 * R;
+    out[1] = fish_weekend_dest(c, w[4]) - lo + h2 * R;
+    out[2] = fish_weekend_dest(c, w[5]) - lo + h3 * R;
 }
 
 // device_getWorkplaceMaxContacts, PandemicSim.cu:3492-3511

@@ -6,8 +6,8 @@
 //   sweep   recover + 16 status bins + ordered infected list, one pass
 //           (kernel_countInfectedStatusAndRecover :2097-2192 + copy_if :2207-2224)
 //   sched   schedule keys + bucket histogram          (:2972-3022 / :2082-2094)
-//   bucket  scan, scatter, per-bucket sort by person id (CUB sort + lower_bound,
-//           :1212-1248 / :1313-1354)
+//   bucket  scan of the histogram (bucket offsets) and a stable LSD radix sort of
+//           the (key, person) entries (CUB sort + lower_bound, :1212-1248, :1313-1354)
 //   infect  contacts and infection draws; the first attempt in (position, slot)
 //           order claims each (victim, strain)        (:3236-3379)
 //   apply   winners write status, day, generation     (:3048-3067)
@@ -192,13 +192,21 @@ cudaError_t launch_household_types(const SimConst &c, uint8_t *types, int32_t *s
 }
 
 // Generic exclusive scan (single pass, decoupled look-back): out[i] = sum in[0..i),
-// out[n] = total.  With clear_in the input is zeroed after it is read.
+// out[n] = total.  With clear_in the input is zeroed after it is read.  With
+// passes > 0, in[] is a histogram over keys 0..n-1 and the scan also accumulates,
+// for each radix pass p, the histogram of the key's 8-bit digit p weighted by the
+// count (digit_hist[p][256]), from which the radix sort takes its digit bases.
 constexpr int kScanThreads = 256, kScanItems = 16, kScanTile = kScanThreads * kScanItems;
+constexpr int kMaxRadixPasses = 4;
 
 __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *in, int32_t *out, int n, int clear_in,
-                                                       LookBack lb, const int *skip)
+                                                       LookBack lb, const int *skip, int passes, int *digit_hist)
 {
     if (skip && *(volatile const int *)skip) return;
+    __shared__ int s_dh[kMaxRadixPasses][256];
+    if (passes > 0) {
+        for (int i = threadIdx.x; i < kMaxRadixPasses * 256; i += blockDim.x) (&s_dh[0][0])[i] = 0;
+    }
     int tile;
     unsigned epoch;
     lookback_begin(lb, tile, epoch);
@@ -218,6 +226,15 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *in, int32_
             if (i < n) ((int32_t *)in)[i] = 0;
         }
     }
+    if (passes > 0) {
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            if (v[k] > 0) {
+                unsigned key = (unsigned)(base + k);
+                for (int p = 0; p < passes; p++) atomicAdd(&s_dh[p][(key >> (8 * p)) & 255u], v[k]);
+            }
+        }
+    }
     int total;
     int excl = block_exclusive_scan<kScanThreads, int>(sum, total);
     __shared__ unsigned s_prefix;
@@ -231,6 +248,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *in, int32_
         run += v[k];
     }
     if (tile == (int)gridDim.x - 1 && threadIdx.x == 0) out[n] = (int)s_prefix + total;
+    if (passes > 0) {
+        for (int p = 0; p < passes; p++) {
+            int c = s_dh[p][threadIdx.x];
+            if (c) atomicAdd(&digit_hist[p * 256 + threadIdx.x], c);
+        }
+    }
     lookback_end(lb);
 }
 
@@ -245,18 +268,31 @@ static LookBack make_lb(unsigned long long *tiles, int tiles_cap, int *error)
 }
 
 cudaError_t launch_scan_exclusive(const int32_t *in, int32_t *out, int n, int clear_in,
-                                  unsigned long long *tiles, int *ticket, int *error,
-                                  const int *skip, cudaStream_t s)
+                                  unsigned long long *tiles, int *ctl, int *error,
+                                  const int *skip, int passes, int *digit_hist, cudaStream_t s)
 {
-    (void)ticket;
     int blocks = std::max(1, div_up(n, kScanTile));
     LookBack lb;
     lb.tiles = tiles;
-    lb.ctl = ticket;
+    lb.ctl = ctl;
     lb.error = error;
-    k_scan<<<blocks, kScanThreads, 0, s>>>(in, out, n, clear_in, lb, skip);
+    k_scan<<<blocks, kScanThreads, 0, s>>>(in, out, n, clear_in, lb, skip, passes, digit_hist);
     count_launch();
     return cudaGetLastError();
+}
+
+// Exclusive scan of each pass's 256-bin digit histogram -> digit bases; clears the
+// histograms for the next sort.
+__global__ void k_digit_bases(int *digit_hist, int *digit_base, int passes, const int *skip)
+{
+    if (skip && *(volatile const int *)skip) return;
+    for (int p = 0; p < passes; p++) {
+        int v = digit_hist[p * 256 + threadIdx.x];
+        int total;
+        int excl = block_exclusive_scan<256, int>(v, total);
+        digit_base[p * 256 + threadIdx.x] = excl;
+        digit_hist[p * 256 + threadIdx.x] = 0;
+    }
 }
 
 // kernel_generateHouseholds (PandemicSim.cu:2490-2531): adults first (AGE_ADULT),
@@ -331,216 +367,190 @@ cudaError_t launch_count_keys(const int32_t *keys, int n, int32_t *count, cudaSt
     return cudaGetLastError();
 }
 
-// Unordered scatter; the per-bucket sort that follows fixes the order.  The
-// cursor (the histogram) counts down to zero, so it is clean for the next build.
-__global__ void k_scatter_identity(const int32_t *keys, int n, const int32_t *offset, int32_t *cursor,
-                                   int32_t *out)
+// ------------------------------------------------------------------ radix sort
+// Bucket tables: the reference sorts (key, person) pairs stably by key and takes
+// lower bounds (CUB radix sort + thrust::lower_bound, PandemicSim.cu:1212-1248,
+// :3835-3862), so every bucket lists its persons in ascending id order.  This stable
+// LSD radix sort over 8-bit digits gives the same table.  Entries enter the first
+// pass in ascending person order; each pass ranks a tile of 4096 entries by digit
+// (warp-blocked, so the rank is stable), finds the tile's global position per digit
+// by a decoupled look-back over earlier tiles (one thread per digit), and writes.
+constexpr int kRadixThreads = 256, kRadixWarps = 8, kRadixItems = 16;
+constexpr int kRadixWarpItems = kRadixItems * 32;
+constexpr int kRadixTile = kRadixThreads * kRadixItems;
+
+enum RadixMode { kRadixFirst = 0, kRadixMiddle = 1, kRadixLast = 2, kRadixOnly = 3 };
+
+// Person id of schedule entry i: the setup table is the identity, weekday entries
+// are hour-major (i < N hour 0, else hour 1), weekend entries person-major (3 per person).
+__device__ __forceinline__ uint32_t entry_person(long long i, int N, int person_mode)
 {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        int k = keys[i];
-        int pos = offset[k] + atomicSub(&cursor[k], 1) - 1;
-        out[pos] = i;
-    }
+    if (person_mode == 0) return (uint32_t)i;
+    if (person_mode == 1) return (uint32_t)(i < N ? i : i - N);
+    return (uint32_t)(i / 3);
 }
 
-cudaError_t launch_scatter_identity(const int32_t *keys, int n, const int32_t *offset, int32_t *cursor,
-                                    int32_t *out, cudaStream_t s)
-{
-    int blocks = std::min(div_up(n, 256), sm_count() * 16);
-    k_scatter_identity<<<std::max(blocks, 1), 256, 0, s>>>(keys, n, offset, cursor, out);
-    count_launch();
-    return cudaGetLastError();
-}
-
-// ------------------------------------------------------------------ bucket sort
-// Buckets list person ids; the reference's stable sort leaves each bucket in
-// ascending id order and ids are unique within a bucket, so sorting each bucket
-// reproduces it exactly.  Size classes: <=16 one thread, <=1024 one warp (bitonic
-// in shared memory), larger one block (bitonic up to kBigSmem ids, then merges).
-constexpr int kSmallMax = 16, kMidMax = 1024, kBigSmem = 16384;
-
-__global__ void k_sort_classify(const int32_t *offset, int buckets, int32_t *people, int32_t *mid_list,
-                                int32_t *big_list, Scalars *sc, const int *skip)
+template <int MODE>
+__global__ void __launch_bounds__(kRadixThreads) k_radix_pass(const uint32_t *__restrict__ keys_in,
+                                                              const uint32_t *__restrict__ vals_in,
+                                                              uint32_t *__restrict__ keys_out,
+                                                              uint32_t *__restrict__ vals_out, int E, int shift,
+                                                              int N, int person_mode,
+                                                              const int *__restrict__ digit_base,
+                                                              uint32_t *status, int *ctl, int *error, const int *skip)
 {
     if (skip && *(volatile const int *)skip) return;
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < buckets; b += gridDim.x * blockDim.x) {
-        int o = offset[b];
-        int n = offset[b + 1] - o;
-        if (n <= 1) continue;
-        if (n <= kSmallMax) {
-            int v[kSmallMax];
-#pragma unroll
-            for (int i = 0; i < kSmallMax; i++) v[i] = i < n ? people[o + i] : INT_MAX;
-            // odd-even transposition network on 16 registers
-#pragma unroll
-            for (int r = 0; r < kSmallMax; r++) {
-#pragma unroll
-                for (int i = (r & 1); i + 1 < kSmallMax; i += 2) {
-                    int a = v[i], bb = v[i + 1];
-                    v[i] = min(a, bb);
-                    v[i + 1] = max(a, bb);
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < kSmallMax; i++)
-                if (i < n) people[o + i] = v[i];
-        } else if (n <= kMidMax) {
-            mid_list[atomicAdd(&sc->mid_count, 1)] = b;
-        } else {
-            big_list[atomicAdd(&sc->big_count, 1)] = b;
-        }
-    }
-}
-
-__device__ __forceinline__ int next_pow2(int n)
-{
-    int p = 1;
-    while (p < n) p <<= 1;
-    return p;
-}
-
-constexpr int kMidWarps = 8;
-
-__global__ void __launch_bounds__(kMidWarps * 32) k_sort_mid(const int32_t *offset, int32_t *people,
-                                                             const int32_t *mid_list, const Scalars *sc,
-                                                             const int *skip)
-{
-    if (skip && *(volatile const int *)skip) return;
-    __shared__ int s_buf[kMidWarps][kMidMax];
+    __shared__ int s_tile;
+    __shared__ int s_hist[kRadixWarps][256];
+    __shared__ int s_base[256];
+    if (threadIdx.x == 0) s_tile = atomicAdd(&ctl[0], 1);
+    for (int i = threadIdx.x; i < kRadixWarps * 256; i += kRadixThreads) (&s_hist[0][0])[i] = 0;
+    __syncthreads();
+    const int tile = s_tile;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int *buf = s_buf[warp];
-    const int count = sc->mid_count;
-    for (int item = blockIdx.x * kMidWarps + warp; item < count; item += gridDim.x * kMidWarps) {
-        int b = mid_list[item];
-        int o = offset[b];
-        int n = offset[b + 1] - o;
-        int P = next_pow2(n);
-        for (int i = lane; i < P; i += 32) buf[i] = i < n ? people[o + i] : INT_MAX;
-        __syncwarp();
-        for (int k = 2; k <= P; k <<= 1) {
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                for (int i = lane; i < P; i += 32) {
-                    int ixj = i ^ j;
-                    if (ixj > i) {
-                        int a = buf[i], c = buf[ixj];
-                        bool up = (i & k) == 0;
-                        if ((a > c) == up) {
-                            buf[i] = c;
-                            buf[ixj] = a;
-                        }
+    const unsigned lt = (1u << lane) - 1u;
+    const long long base = (long long)tile * kRadixTile + (long long)warp * kRadixWarpItems + lane;
+    uint32_t key[kRadixItems], val[kRadixItems];
+#pragma unroll
+    for (int j = 0; j < kRadixItems; j++) {
+        const long long i = base + 32 * j;
+        const bool ok = i < E;
+        key[j] = ok ? keys_in[i] : 0u;
+        if (MODE == kRadixFirst || MODE == kRadixOnly) val[j] = entry_person(i, N, person_mode);
+        else val[j] = ok ? vals_in[i] : 0u;
+    }
+    // per-warp digit counts (each warp owns one row; its rounds run in order)
+#pragma unroll
+    for (int j = 0; j < kRadixItems; j++) {
+        const bool ok = base + 32 * j < E;
+        const unsigned d = (key[j] >> shift) & 255u;
+        const unsigned peers = __match_any_sync(0xffffffffu, ok ? d : 256u + lane);
+        if (ok && (peers & lt) == 0) s_hist[warp][d] += __popc(peers);
+    }
+    __syncthreads();
+    {
+        // thread d: exclusive bases of the warps for digit d, then the look-back
+        const int d = threadIdx.x;
+        int run = 0;
+#pragma unroll
+        for (int w = 0; w < kRadixWarps; w++) {
+            int c = s_hist[w][d];
+            s_hist[w][d] = run;
+            run += c;
+        }
+        volatile uint32_t *st = status;
+        int excl = 0;
+        if (tile == 0) {
+            st[d] = (2u << 30) | (uint32_t)run;
+        } else {
+            st[(size_t)tile * 256 + d] = (1u << 30) | (uint32_t)run;
+            int t = tile - 1;
+            long long spins = 0;
+            while (t >= 0) {
+                const uint32_t w = st[(size_t)t * 256 + d];
+                const uint32_t flag = w >> 30;
+                if (flag == 0) {
+                    if (++spins > kSpinLimit) {
+                        atomicExch(error, 2);
+                        break;
                     }
+                    __nanosleep(32);
+                    continue;
                 }
-                __syncwarp();
+                excl += (int)(w & 0x3FFFFFFFu);
+                if (flag == 2) break;
+                t--;
             }
+            st[(size_t)tile * 256 + d] = (2u << 30) | (uint32_t)(excl + run);
         }
-        for (int i = lane; i < n; i += 32) people[o + i] = buf[i];
+        s_base[d] = digit_base[d] + excl;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kRadixItems; j++) {
+        const bool ok = base + 32 * j < E;
+        const unsigned d = (key[j] >> shift) & 255u;
+        const unsigned peers = __match_any_sync(0xffffffffu, ok ? d : 256u + lane);
+        const int wbase = ok ? s_hist[warp][d] : 0;
+        __syncwarp();
+        if (ok) {
+            const int pos = s_base[d] + wbase + __popc(peers & lt);
+            if (MODE == kRadixFirst || MODE == kRadixMiddle) keys_out[pos] = key[j];
+            vals_out[pos] = val[j];
+            if ((peers & lt) == 0) s_hist[warp][d] = wbase + __popc(peers);
+        }
         __syncwarp();
     }
-}
-
-constexpr int kBigThreads = 1024;
-
-__device__ void block_bitonic(int *buf, int P)
-{
-    for (int k = 2; k <= P; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < P; i += blockDim.x) {
-                int ixj = i ^ j;
-                if (ixj > i) {
-                    int a = buf[i], c = buf[ixj];
-                    bool up = (i & k) == 0;
-                    if ((a > c) == up) {
-                        buf[i] = c;
-                        buf[ixj] = a;
-                    }
-                }
-            }
-            __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const int fin = atomicAdd(&ctl[1], 1);
+        if (fin == (int)gridDim.x - 1) {
+            ctl[0] = 0;
+            ctl[1] = 0;
+            __threadfence();
         }
     }
 }
 
-// Rank of x among sorted distinct values r[0..m): number of elements < x.
-__device__ __forceinline__ int lower_rank(const int32_t *r, int m, int x)
+int radix_passes(int buckets)
 {
-    int lo = 0, hi = m;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (r[mid] < x) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
+    int bits = 0;
+    while (bits < 31 && (1ll << bits) < (long long)buckets) bits++;
+    return std::max(1, (bits + 7) / 8);
 }
 
-__global__ void __launch_bounds__(kBigThreads) k_sort_big(const int32_t *offset, int32_t *people, int32_t *tmp,
-                                                          const int32_t *big_list, const Scalars *sc,
-                                                          const int *skip)
+cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
 {
-    if (skip && *(volatile const int *)skip) return;
-    extern __shared__ int s_big[];
-    const int count = sc->big_count;
-    for (int item = blockIdx.x; item < count; item += gridDim.x) {
-        int b = big_list[item];
-        int o = offset[b];
-        int n = offset[b + 1] - o;
-        int32_t *a = people + o;
-        // sort chunks of kBigSmem in shared memory
-        for (int c0 = 0; c0 < n; c0 += kBigSmem) {
-            int m = min(kBigSmem, n - c0);
-            int P = next_pow2(m);
-            for (int i = threadIdx.x; i < P; i += blockDim.x) s_big[i] = i < m ? a[c0 + i] : INT_MAX;
-            __syncthreads();
-            block_bitonic(s_big, P);
-            for (int i = threadIdx.x; i < m; i += blockDim.x) a[c0 + i] = s_big[i];
-            __syncthreads();
-        }
-        // merge runs pairwise: each element's output index is its own index plus its
-        // rank in the partner run (values are distinct).
-        int32_t *t = tmp + o;
-        for (int w = kBigSmem; w < n; w <<= 1) {
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                int run = i / w;
-                int start = run * w;
-                int pstart, plen, base;
-                if ((run & 1) == 0) {
-                    pstart = start + w;
-                    plen = max(0, min(w, n - pstart));
-                    base = start;
-                } else {
-                    pstart = start - w;
-                    plen = w;
-                    base = pstart;
-                }
-                int own = i - start;
-                int r = plen > 0 ? lower_rank(a + pstart, plen, a[i]) : 0;
-                t[base + own + r] = a[i];
-            }
-            __syncthreads();
-            for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = t[i];
-            __syncthreads();
-        }
+    const int P = radix_passes(r.buckets);
+    const int tiles = std::max(1, div_up(r.E, kRadixTile));
+    const uint32_t *kin = r.keys;
+    const uint32_t *vin = nullptr;
+    for (int p = 0; p < P; p++) {
+        cudaError_t e = cudaMemsetAsync(r.status, 0, (size_t)tiles * 256 * sizeof(uint32_t), s);
+        if (e != cudaSuccess) return e;
+        uint32_t *kout = (p & 1) ? r.k1 : r.k0;
+        uint32_t *vout = (p == P - 1) ? r.out : ((p & 1) ? r.v1 : r.v0);
+        const int *db = r.digit_base + 256 * p;
+        const int shift = 8 * p;
+        if (P == 1)
+            k_radix_pass<kRadixOnly><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, r.N,
+                                                                    r.person_mode, db, r.status, r.ctl, r.error, r.skip);
+        else if (p == 0)
+            k_radix_pass<kRadixFirst><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, r.N,
+                                                                     r.person_mode, db, r.status, r.ctl, r.error, r.skip);
+        else if (p == P - 1)
+            k_radix_pass<kRadixLast><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, r.N,
+                                                                    r.person_mode, db, r.status, r.ctl, r.error, r.skip);
+        else
+            k_radix_pass<kRadixMiddle><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, r.N,
+                                                                      r.person_mode, db, r.status, r.ctl, r.error, r.skip);
+        count_launch();
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        kin = kout;
+        vin = vout;
     }
+    return cudaSuccess;
 }
 
-cudaError_t launch_sort_buckets(const int32_t *offset, int buckets, int32_t *people, int32_t *tmp,
-                                int32_t *mid_list, int32_t *big_list, Scalars *sc, const int *skip,
-                                cudaStream_t s)
+// Count, scan (+digit histograms), digit bases and radix passes: the bucket table of
+// `E` keys in [0, buckets).  counts must be zero on entry and is zero on exit.
+cudaError_t launch_bucket_table(const RadixArgs &r, int32_t *counts, bool count_keys, int32_t *offset,
+                                unsigned long long *tiles, int *lb_ctl, int *digit_hist, cudaStream_t s)
 {
-    cudaError_t e = cudaMemsetAsync(&sc->mid_count, 0, 2 * sizeof(int), s);
+    const int P = radix_passes(r.buckets);
+    if (count_keys) {
+        cudaError_t e = launch_count_keys((const int32_t *)r.keys, r.E, counts, s);
+        if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = launch_scan_exclusive(counts, offset, r.buckets, 1, tiles, lb_ctl, r.error, r.skip, P,
+                                          digit_hist, s);
     if (e != cudaSuccess) return e;
-    int blocks = std::max(1, std::min(div_up(buckets, 256), sm_count() * 32));
-    k_sort_classify<<<blocks, 256, 0, s>>>(offset, buckets, people, mid_list, big_list, sc, skip);
+    k_digit_bases<<<1, 256, 0, s>>>(digit_hist, (int *)r.digit_base, P, r.skip);
     count_launch();
-    k_sort_mid<<<sm_count() * 4, kMidWarps * 32, 0, s>>>(offset, people, mid_list, sc, skip);
-    count_launch();
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_sort_big, cudaFuncAttributeMaxDynamicSharedMemorySize, kBigSmem * (int)sizeof(int));
-        attr = true;
-    }
-    k_sort_big<<<sm_count(), kBigThreads, kBigSmem * sizeof(int), s>>>(offset, people, tmp, big_list, sc, skip);
-    count_launch();
-    return cudaGetLastError();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_radix_sort(r, s);
 }
 
 // setup_initializeStatusArrays (PandemicSim.cu:3654-3664): S/S, day 255/255, gen 255.
@@ -738,12 +748,15 @@ cudaError_t launch_sweep(const SimConst &c, const DevArrays &d, int day, cudaStr
 
 // Weekday schedule (kernel_assignWeekdayAfterschoolAndErrands, PandemicSim.cu:2972-3022):
 // counter E0 + g -> persons 2g, 2g+1.  Hour-0 keys at [0,N), hour-1 keys at [N,2N).
+// Weekday destinations lie in [lo, L), lo = first location of type 8 (afterschool),
+// so the bucket index is hour * R + dest - lo with R = L - lo (order-preserving).
 __global__ void k_sched_weekday(SimConst c, const uint8_t *age, int32_t *keys, int32_t *count, const Scalars *sc)
 {
     if (sc->done) return;
     const TfKey key = make_key(c);
     const unsigned long long E0 = sc->errand_offset;
     const int N = c.N, G = N / 2;
+    const int lo = c.type_offset[8], R = c.L - lo;
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x) {
         uint32_t w[4];
         tf2x64(key, E0 + (uint64_t)g, w);
@@ -754,11 +767,11 @@ __global__ void k_sched_weekday(SimConst c, const uint8_t *age, int32_t *keys, i
                 bool adult = age[p] == 5;
                 int d1 = fish_weekday_dest(c, w[2 * k], adult);
                 int d2 = adult ? fish_weekday_dest(c, w[2 * k + 1], true) : d1;
-                d2 += c.L;
-                keys[p] = d1;
-                keys[N + p] = d2;
-                atomicAdd(&count[d1], 1);
-                atomicAdd(&count[d2], 1);
+                const int k1 = d1 - lo, k2 = R + d2 - lo;
+                keys[p] = k1;
+                keys[N + p] = k2;
+                atomicAdd(&count[k1], 1);
+                atomicAdd(&count[k2], 1);
             }
         }
     }
@@ -771,9 +784,10 @@ __global__ void k_sched_weekend(SimConst c, int32_t *keys, int32_t *count, const
     if (sc->done) return;
     const TfKey key = make_key(c);
     const unsigned long long E0 = sc->errand_offset;
+    const int lo = c.type_offset[9], R = c.L - lo;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < c.N; p += gridDim.x * blockDim.x) {
         int d[3];
-        weekend_errands(c, key, E0 + 2ull * (unsigned long long)p, d);
+        weekend_errands(c, key, E0 + 2ull * (unsigned long long)p, lo, R, d);
         keys[3 * (size_t)p + 0] = d[0];
         keys[3 * (size_t)p + 1] = d[1];
         keys[3 * (size_t)p + 2] = d[2];
@@ -781,6 +795,11 @@ __global__ void k_sched_weekend(SimConst c, int32_t *keys, int32_t *count, const
         atomicAdd(&count[d[1]], 1);
         atomicAdd(&count[d[2]], 1);
     }
+}
+
+int day_buckets(const SimConst &c, bool weekend)
+{
+    return weekend ? 10 * (c.L - c.type_offset[9]) : 2 * (c.L - c.type_offset[8]);
 }
 
 cudaError_t launch_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s)
@@ -796,44 +815,40 @@ cudaError_t launch_schedule(const SimConst &c, const DevArrays &d, bool weekend,
     return cudaGetLastError();
 }
 
+static RadixArgs day_radix_args(const SimConst &c, const DevArrays &d, bool weekend)
+{
+    RadixArgs r;
+    r.keys = (const uint32_t *)d.keys;
+    r.E = (weekend ? 3 : 2) * c.N;
+    r.buckets = day_buckets(c, weekend);
+    r.N = c.N;
+    r.person_mode = weekend ? 2 : 1;
+    r.k0 = d.rk0; r.v0 = d.rv0; r.k1 = d.rk1; r.v1 = d.rv1;
+    r.out = (uint32_t *)d.bkt_people;
+    r.digit_base = d.digit_base;
+    r.status = d.radix_status;
+    r.ctl = d.radix_ctl;
+    r.error = &d.sc->error;
+    r.skip = &d.sc->done;
+    return r;
+}
+
 cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s)
 {
-    const int B = (weekend ? 10 : 2) * c.L;
-    LookBack lb = make_lb(d.tiles, d.tiles_cap, &d.sc->error);
-    int blocks = std::max(1, div_up(B, kScanTile));
-    k_scan<<<blocks, kScanThreads, 0, s>>>(d.bkt_count, d.bkt_offset, B, 0, lb, &d.sc->done);
+    RadixArgs r = day_radix_args(c, d, weekend);
+    const int P = radix_passes(r.buckets);
+    cudaError_t e = launch_scan_exclusive(d.bkt_count, d.bkt_offset, r.buckets, 1, d.tiles,
+                                          (int *)(d.tiles + d.tiles_cap), &d.sc->error, &d.sc->done, P,
+                                          d.digit_hist, s);
+    if (e != cudaSuccess) return e;
+    k_digit_bases<<<1, 256, 0, s>>>(d.digit_hist, d.digit_base, P, &d.sc->done);
     count_launch();
     return cudaGetLastError();
 }
 
-__global__ void k_scatter_sched(const int32_t *keys, int N, int weekend, const int32_t *offset, int32_t *cursor,
-                                int32_t *people, const Scalars *sc)
+cudaError_t launch_bucket_sort(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s)
 {
-    if (sc->done) return;
-    const long long E = (long long)(weekend ? 3 : 2) * N;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < E; e += (long long)gridDim.x * blockDim.x) {
-        int k = keys[e];
-        int person = weekend ? (int)(e / 3) : (int)(e < N ? e : e - N);
-        int pos = offset[k] + atomicSub(&cursor[k], 1) - 1;
-        people[pos] = person;
-    }
-}
-
-cudaError_t launch_scatter_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s)
-{
-    const long long E = (long long)(weekend ? 3 : 2) * c.N;
-    int blocks = (int)std::min<long long>((E + 255) / 256, (long long)sm_count() * 32);
-    k_scatter_sched<<<std::max(1, blocks), 256, 0, s>>>(d.keys, c.N, weekend ? 1 : 0, d.bkt_offset, d.bkt_count,
-                                                        d.bkt_people, d.sc);
-    count_launch();
-    return cudaGetLastError();
-}
-
-cudaError_t launch_sort_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s)
-{
-    const int B = (weekend ? 10 : 2) * c.L;
-    return launch_sort_buckets(d.bkt_offset, B, d.bkt_people, d.sort_tmp, d.mid_list, d.big_list, d.sc,
-                               &d.sc->done, s);
+    return launch_radix_sort(day_radix_args(c, d, weekend), s);
 }
 
 // ------------------------------------------------------------------ infection

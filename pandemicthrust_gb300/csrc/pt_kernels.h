@@ -56,13 +56,15 @@ struct DevArrays {
     int32_t *workplace;       // N
     int32_t *wp_people;       // N
     int32_t *wp_offset;       // L+1
-    int32_t *keys;            // 3N schedule keys
-    int32_t *bkt_offset;      // 10L+1
-    int32_t *bkt_count;       // 10L (histogram, then scatter cursor)
-    int32_t *bkt_people;      // 3N
-    int32_t *sort_tmp;        // 3N scratch for the large-bucket merge
-    int32_t *mid_list;        // 10L bucket ids for the warp sort
-    int32_t *big_list;        // 10L bucket ids for the block sort
+    int32_t *keys;            // 3N schedule keys (compact bucket indices)
+    int32_t *bkt_offset;      // buckets+1 (at most 10L+1)
+    int32_t *bkt_count;       // buckets histogram, zero between uses
+    int32_t *bkt_people;      // 3N person ids bucket by bucket, ascending in each
+    uint32_t *rk0, *rv0, *rk1, *rv1;  // 3N each: radix ping-pong keys/values
+    uint32_t *radix_status;   // ceil(3N/4096) x 256 look-back words per pass
+    int *radix_ctl;           // ticket, finished
+    int *digit_hist;          // 4 x 256
+    int *digit_base;          // 4 x 256
     int32_t *infected;        // N ascending infected ids
     unsigned long long *claim;// 2N (victim, strain) -> min attempt key
     int32_t *new_list;        // 2N first claims of the day
@@ -78,17 +80,30 @@ int sm_count();
 cudaError_t launch_household_types(const SimConst &c, uint8_t *types, int32_t *sizes, int *adults,
                                    cudaStream_t s);
 cudaError_t launch_scan_exclusive(const int32_t *in, int32_t *out, int n, int clear_in,
-                                  unsigned long long *tiles, int *ticket, int *error,
-                                  const int *skip, cudaStream_t s);
+                                  unsigned long long *tiles, int *ctl, int *error,
+                                  const int *skip, int passes, int *digit_hist, cudaStream_t s);
 cudaError_t launch_generate_households(const SimConst &c, const uint8_t *types, const int32_t *hh_offset,
                                        int32_t *household, uint8_t *age, cudaStream_t s);
 cudaError_t launch_assign_workplaces(const SimConst &c, uint8_t *age, int32_t *workplace, cudaStream_t s);
 cudaError_t launch_count_keys(const int32_t *keys, int n, int32_t *count, cudaStream_t s);
-cudaError_t launch_scatter_identity(const int32_t *keys, int n, const int32_t *offset, int32_t *cursor,
-                                    int32_t *out, cudaStream_t s);
-cudaError_t launch_sort_buckets(const int32_t *offset, int buckets, int32_t *people, int32_t *tmp,
-                                int32_t *mid_list, int32_t *big_list, Scalars *sc, const int *skip,
-                                cudaStream_t s);
+
+// Stable LSD radix sort of E keys in [0, buckets) with implicit person values
+// (person_mode 0: entry i is person i; 1: weekday hour-major; 2: weekend 3 per person).
+struct RadixArgs {
+    const uint32_t *keys;
+    int E, buckets, N, person_mode;
+    uint32_t *k0, *v0, *k1, *v1, *out;
+    const int *digit_base;
+    uint32_t *status;
+    int *ctl;
+    int *error;
+    const int *skip;
+};
+int radix_passes(int buckets);
+cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s);
+// count (optional) + scan + digit bases + radix passes: a complete bucket table
+cudaError_t launch_bucket_table(const RadixArgs &r, int32_t *counts, bool count_keys, int32_t *offset,
+                                unsigned long long *tiles, int *lb_ctl, int *digit_hist, cudaStream_t s);
 cudaError_t launch_init_status(int N, uint32_t *state, uint8_t *gen_p, uint8_t *gen_s,
                                unsigned long long *claim, cudaStream_t s);
 cudaError_t launch_seed_infected(const int32_t *seeds, int P, int S, uint32_t *state, uint8_t *gen_p,
@@ -97,9 +112,9 @@ cudaError_t launch_seed_infected(const int32_t *seeds, int P, int S, uint32_t *s
 // ---- day
 cudaError_t launch_sweep(const SimConst &c, const DevArrays &d, int day, cudaStream_t s);
 cudaError_t launch_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
+int day_buckets(const SimConst &c, bool weekend);
 cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
-cudaError_t launch_scatter_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
-cudaError_t launch_sort_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
+cudaError_t launch_bucket_sort(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
 cudaError_t launch_infect(const SimConst &c, const DevArrays &d, bool weekend, int day, cudaStream_t s);
 cudaError_t launch_apply(const DevArrays &d, int day, cudaStream_t s);
 

@@ -215,8 +215,8 @@ pt_status pt_setup(pt_sim *s)
 
     // households: types and sizes, exclusive scan -> offsets and N
     CK(ptk::launch_household_types(c, types, sizes, &d.sc->adults, s->stream), "household_types");
-    CK(ptk::launch_scan_exclusive(sizes, d.hh_offset, H, 0, d.tiles, ctl, &d.sc->error, nullptr, s->stream),
-       "household scan");
+    CK(ptk::launch_scan_exclusive(sizes, d.hh_offset, H, 0, d.tiles, ctl, &d.sc->error, nullptr, 0, nullptr,
+                                  s->stream), "household scan");
     int hN = 0, hA = 0;
     CK(pt_memcpy(s, &hN, d.hh_offset + H, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "N copy");
     CK(pt_memcpy(s, &hA, &d.sc->adults, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "adults copy");
@@ -229,16 +229,21 @@ pt_status pt_setup(pt_sim *s)
     const int P = s->params.initial_pandemic, S = s->params.initial_seasonal;
     if ((long long)P + S > N) return fail(s, PT_ERR_ARG, "more initial infected than persons");
 
+    if ((long long)N * 3 >= (1ll << 30)) return fail(s, PT_ERR_ARG, "population too large (3N must stay below 2^30)");
+
     // arena of per-person and per-location arrays
     const size_t n = (size_t)N, B = 10 * (size_t)L;
+    const size_t radix_tiles = (3 * n + 4095) / 4096 + 1;
     size_t bytes = 0;
     bytes += round256(n * 4);                 // state
     bytes += 3 * round256(n);                 // gen_p, gen_s, age
     bytes += round256(n * 4) * 3;             // household, workplace, wp_people
     bytes += round256(((size_t)L + 1) * 4);   // wp_offset
-    bytes += round256(3 * n * 4) * 3;         // keys, bkt_people, sort_tmp
+    bytes += round256(3 * n * 4) * 6;         // keys, bkt_people, radix k0/v0/k1/v1
     bytes += round256((B + 1) * 4);           // bkt_offset
-    bytes += round256(B * 4) * 3;             // bkt_count, mid_list, big_list
+    bytes += round256(B * 4);                 // bkt_count
+    bytes += round256(radix_tiles * 256 * 4); // radix look-back words
+    bytes += round256(8 * 4) + 2 * round256(4 * 256 * 4);  // radix ctl, digit hist/base
     bytes += round256(n * 4);                 // infected
     bytes += round256(2 * n * 8);             // claim
     bytes += round256(2 * n * 4);             // new_list
@@ -256,27 +261,46 @@ pt_status pt_setup(pt_sim *s)
     d.wp_offset = a.take<int32_t>((size_t)L + 1);
     d.keys = a.take<int32_t>(3 * n);
     d.bkt_people = a.take<int32_t>(3 * n);
-    d.sort_tmp = a.take<int32_t>(3 * n);
+    d.rk0 = a.take<uint32_t>(3 * n);
+    d.rv0 = a.take<uint32_t>(3 * n);
+    d.rk1 = a.take<uint32_t>(3 * n);
+    d.rv1 = a.take<uint32_t>(3 * n);
     d.bkt_offset = a.take<int32_t>(B + 1);
     d.bkt_count = a.take<int32_t>(B);
-    d.mid_list = a.take<int32_t>(B);
-    d.big_list = a.take<int32_t>(B);
+    d.radix_status = a.take<uint32_t>(radix_tiles * 256);
+    d.radix_ctl = a.take<int>(8);
+    d.digit_hist = a.take<int>(4 * 256);
+    d.digit_base = a.take<int>(4 * 256);
     d.infected = a.take<int32_t>(n);
     d.claim = a.take<unsigned long long>(2 * n);
     d.new_list = a.take<int32_t>(2 * n);
     s->d_seeds = a.take<int32_t>((size_t)(P + S + 1));
     CK(cudaMemsetAsync(d.bkt_count, 0, B * 4, s->stream), "memset counts");
+    CK(cudaMemsetAsync(d.radix_ctl, 0, 8 * 4, s->stream), "memset radix ctl");
+    CK(cudaMemsetAsync(d.digit_hist, 0, 4 * 256 * 4, s->stream), "memset digit hist");
 
     // households -> persons, then workplaces and schools (setup_assignWorkplaces)
     CK(ptk::launch_generate_households(c, types, d.hh_offset, d.household, d.age, s->stream), "households");
     CK(ptk::launch_assign_workplaces(c, d.age, d.workplace, s->stream), "workplaces");
-    // workplace table: count, scan, scatter, per-bucket sort
-    CK(ptk::launch_count_keys(d.workplace, N, d.bkt_count, s->stream), "wp count");
-    CK(ptk::launch_scan_exclusive(d.bkt_count, d.wp_offset, L, 0, d.tiles, ctl, &d.sc->error, nullptr, s->stream),
-       "wp scan");
-    CK(ptk::launch_scatter_identity(d.workplace, N, d.wp_offset, d.bkt_count, d.wp_people, s->stream), "wp scatter");
-    CK(ptk::launch_sort_buckets(d.wp_offset, L, d.wp_people, d.sort_tmp, d.mid_list, d.big_list, d.sc, nullptr,
-                                s->stream), "wp sort");
+    // workplace table: person ids stably sorted by workplace, with offsets
+    // (setup_assignWorkplaces' radix sort + lower_bound, PandemicSim.cu:3835-3862)
+    {
+        ptk::RadixArgs r;
+        r.keys = (const uint32_t *)d.workplace;
+        r.E = N;
+        r.buckets = L;
+        r.N = N;
+        r.person_mode = 0;
+        r.k0 = d.rk0; r.v0 = d.rv0; r.k1 = d.rk1; r.v1 = d.rv1;
+        r.out = (uint32_t *)d.wp_people;
+        r.digit_base = d.digit_base;
+        r.status = d.radix_status;
+        r.ctl = d.radix_ctl;
+        r.error = &d.sc->error;
+        r.skip = nullptr;
+        CK(ptk::launch_bucket_table(r, d.bkt_count, true, d.wp_offset, d.tiles, ctl, d.digit_hist, s->stream),
+           "workplace table");
+    }
     // initial infected: rand() % N draws continue the seed sequence (PandemicSim.cu:708-758)
     s->seed_list = pth::unique_numbers(*s->rng, P + S, N);
     int derr = 0;
@@ -299,14 +323,14 @@ pt_status pt_reset_epidemic(pt_sim *s)
 }
 
 // Stage boundaries recorded per day when timing is on.
-enum { kStSweep, kStSchedule, kStScan, kStScatter, kStSort, kStInfect, kStApply, kStages };
+enum { kStSweep, kStSchedule, kStScan, kStRadix, kStInfect, kStApply, kStages };
 
 static cudaEvent_t stage_event(pt_sim *s, int day, int k)
 {
     return s->day_events[(size_t)day * (kStages + 1) + k];
 }
 
-// Enqueues one day: sweep, schedule, bucket build (scan, scatter, sort), infection,
+// Enqueues one day: sweep, schedule, bucket build (scan, radix sort), infection,
 // apply.  Every kernel after the sweep skips itself on the device when the day
 // counted no infected.
 static pt_status enqueue_day(pt_sim *s, int day)
@@ -323,14 +347,12 @@ static pt_status enqueue_day(pt_sim *s, int day)
     if (t) cudaEventRecord(stage_event(s, day, 2), st);
     CK(ptk::launch_bucket_scan(c, d, weekend, st), "bucket scan");
     if (t) cudaEventRecord(stage_event(s, day, 3), st);
-    CK(ptk::launch_scatter_schedule(c, d, weekend, st), "bucket scatter");
+    CK(ptk::launch_bucket_sort(c, d, weekend, st), "bucket sort");
     if (t) cudaEventRecord(stage_event(s, day, 4), st);
-    CK(ptk::launch_sort_schedule(c, d, weekend, st), "bucket sort");
-    if (t) cudaEventRecord(stage_event(s, day, 5), st);
     CK(ptk::launch_infect(c, d, weekend, day, st), "infect");
-    if (t) cudaEventRecord(stage_event(s, day, 6), st);
+    if (t) cudaEventRecord(stage_event(s, day, 5), st);
     CK(ptk::launch_apply(d, day, st), "apply");
-    if (t) cudaEventRecord(stage_event(s, day, 7), st);
+    if (t) cudaEventRecord(stage_event(s, day, 6), st);
     if (t) s->timed_days.push_back(day);
     return PT_OK;
 }
@@ -548,6 +570,12 @@ pt_status pt_get_population(pt_sim *s, int32_t *household, int32_t *household_of
     return PT_OK;
 }
 
+// The device keeps each day's buckets in compact form: errand destinations of a
+// day all lie in [lo, L) (lo = first location of type 8 on weekdays, type 9 on
+// weekends), so bucket hour*R + dest - lo (R = L - lo) replaces the reference's key
+// hour*L + dest.  This copies the tables back in the reference's layout: keys
+// hour*L + dest and offsets over all 2L (10L) keys, offsets[k] = number of entries
+// with a smaller key.
 pt_status pt_get_day_tables(pt_sim *s, int32_t *infected, int32_t *keys, int32_t *people, int32_t *offsets,
                             int *entries, int *buckets)
 {
@@ -558,14 +586,30 @@ pt_status pt_get_day_tables(pt_sim *s, int32_t *infected, int32_t *keys, int32_t
     CK(pt_memcpy_sync(s, &sc, s->d.sc, sizeof(sc), cudaMemcpyDeviceToHost), "scalars");
     const int day = sc.day;
     const bool weekend = (day % 7) >= 5;
-    const int E = (weekend ? 3 : 2) * s->c.N, B = (weekend ? 10 : 2) * s->c.L;
+    const int L = s->c.L, hours = weekend ? 10 : 2;
+    const int lo = s->c.type_offset[weekend ? 9 : 8], R = L - lo;
+    const int E = (weekend ? 3 : 2) * s->c.N, B = hours * L;
+    const int Bc = ptk::day_buckets(s->c, weekend);
     if (entries) *entries = E;
     if (buckets) *buckets = B;
     if (infected && sc.infected > 0)
         CK(pt_memcpy_sync(s, infected, s->d.infected, (size_t)sc.infected * 4, cudaMemcpyDeviceToHost), "copy");
-    if (keys) CK(pt_memcpy_sync(s, keys, s->d.keys, (size_t)E * 4, cudaMemcpyDeviceToHost), "copy");
+    if (keys) {
+        CK(pt_memcpy_sync(s, keys, s->d.keys, (size_t)E * 4, cudaMemcpyDeviceToHost), "copy");
+        for (int i = 0; i < E; i++) {
+            int h = keys[i] / R, loc = keys[i] % R + lo;
+            keys[i] = h * L + loc;
+        }
+    }
     if (people) CK(pt_memcpy_sync(s, people, s->d.bkt_people, (size_t)E * 4, cudaMemcpyDeviceToHost), "copy");
-    if (offsets) CK(pt_memcpy_sync(s, offsets, s->d.bkt_offset, ((size_t)B + 1) * 4, cudaMemcpyDeviceToHost), "copy");
+    if (offsets) {
+        std::vector<int32_t> co((size_t)Bc + 1);
+        CK(pt_memcpy_sync(s, co.data(), s->d.bkt_offset, ((size_t)Bc + 1) * 4, cudaMemcpyDeviceToHost), "copy");
+        for (int h = 0; h < hours; h++)
+            for (int loc = 0; loc < L; loc++)
+                offsets[(size_t)h * L + loc] = loc < lo ? co[(size_t)h * R] : co[(size_t)h * R + loc - lo];
+        offsets[B] = E;
+    }
     return PT_OK;
 }
 
