@@ -390,12 +390,28 @@ __device__ __forceinline__ uint32_t entry_person(long long i, int N, int person_
     return (uint32_t)(i / 3);
 }
 
+// Lanes of the warp holding the same digit as this lane (among lanes in `valid`),
+// from one ballot per digit bit: constant cost, unlike a match over 256 values.
+__device__ __forceinline__ unsigned digit_peers(unsigned d, int nbits, unsigned valid)
+{
+    unsigned peers = valid;
+#pragma unroll
+    for (int b = 0; b < 8; b++) {
+        if (b < nbits) {
+            const unsigned bit = (d >> b) & 1u;
+            const unsigned bal = __ballot_sync(0xffffffffu, bit);
+            peers &= bit ? bal : ~bal;
+        }
+    }
+    return peers;
+}
+
 template <int MODE>
-__global__ void __launch_bounds__(kRadixThreads) k_radix_pass(const uint32_t *__restrict__ keys_in,
+__global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t *__restrict__ keys_in,
                                                               const uint32_t *__restrict__ vals_in,
                                                               uint32_t *__restrict__ keys_out,
                                                               uint32_t *__restrict__ vals_out, int E, int shift,
-                                                              int N, int person_mode,
+                                                              int nbits, int N, int person_mode,
                                                               const int *__restrict__ digit_base,
                                                               uint32_t *status, int *ctl, int *error, const int *skip)
 {
@@ -424,7 +440,7 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_pass(const uint32_t *__
     for (int j = 0; j < kRadixItems; j++) {
         const bool ok = base + 32 * j < E;
         const unsigned d = (key[j] >> shift) & 255u;
-        const unsigned peers = __match_any_sync(0xffffffffu, ok ? d : 256u + lane);
+        const unsigned peers = digit_peers(d, nbits, __ballot_sync(0xffffffffu, ok));
         if (ok && (peers & lt) == 0) s_hist[warp][d] += __popc(peers);
     }
     __syncthreads();
@@ -470,7 +486,7 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_pass(const uint32_t *__
     for (int j = 0; j < kRadixItems; j++) {
         const bool ok = base + 32 * j < E;
         const unsigned d = (key[j] >> shift) & 255u;
-        const unsigned peers = __match_any_sync(0xffffffffu, ok ? d : 256u + lane);
+        const unsigned peers = digit_peers(d, nbits, __ballot_sync(0xffffffffu, ok));
         const int wbase = ok ? s_hist[warp][d] : 0;
         __syncwarp();
         if (ok) {
@@ -492,16 +508,19 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_pass(const uint32_t *__
     }
 }
 
-int radix_passes(int buckets)
+static int key_bits(int buckets)
 {
     int bits = 0;
     while (bits < 31 && (1ll << bits) < (long long)buckets) bits++;
-    return std::max(1, (bits + 7) / 8);
+    return bits;
 }
+
+int radix_passes(int buckets) { return std::max(1, (key_bits(buckets) + 7) / 8); }
 
 cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
 {
     const int P = radix_passes(r.buckets);
+    const int bits = key_bits(r.buckets);
     const int tiles = std::max(1, div_up(r.E, kRadixTile));
     const uint32_t *kin = r.keys;
     const uint32_t *vin = nullptr;
@@ -512,17 +531,18 @@ cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
         uint32_t *vout = (p == P - 1) ? r.out : ((p & 1) ? r.v1 : r.v0);
         const int *db = r.digit_base + 256 * p;
         const int shift = 8 * p;
+        const int nbits = std::max(1, std::min(8, bits - shift));
         if (P == 1)
-            k_radix_pass<kRadixOnly><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, r.N,
+            k_radix_pass<kRadixOnly><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, nbits, r.N,
                                                                     r.person_mode, db, r.status, r.ctl, r.error, r.skip);
         else if (p == 0)
-            k_radix_pass<kRadixFirst><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, r.N,
+            k_radix_pass<kRadixFirst><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, nbits, r.N,
                                                                      r.person_mode, db, r.status, r.ctl, r.error, r.skip);
         else if (p == P - 1)
-            k_radix_pass<kRadixLast><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, r.N,
+            k_radix_pass<kRadixLast><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, nbits, r.N,
                                                                     r.person_mode, db, r.status, r.ctl, r.error, r.skip);
         else
-            k_radix_pass<kRadixMiddle><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, r.N,
+            k_radix_pass<kRadixMiddle><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, nbits, r.N,
                                                                       r.person_mode, db, r.status, r.ctl, r.error, r.skip);
         count_launch();
         e = cudaGetLastError();
