@@ -146,6 +146,30 @@ uint64_t pt_launch_count(void);
 /* Bytes this simulation has copied host-to-device and device-to-host so far. */
 pt_status pt_transfer_bytes(const pt_sim *sim, uint64_t *h2d, uint64_t *d2h);
 
+/* Largest input pt_bucket_table_static accepts: its scratch space is compiled into
+ * the library, about 21 MiB of device memory held by every GPU that loads it. */
+#define PT_STATIC_TABLE_MAX_ENTRIES (1 << 20)
+#define PT_STATIC_TABLE_MAX_BUCKETS (1 << 20)
+
+/* Builds a bucket table without allocating any device memory.  No counterpart in
+ * the reference: it is for callers that cannot call cudaMalloc on their path, such
+ * as a host that passes in device buffers carved from its own pool and forbids any
+ * other allocation, or a loop that keeps other streams busy, where cudaMalloc and
+ * cudaFree would synchronise the whole device and stall that work.
+ *
+ * keys (device, n entries, each in [0, buckets)) -> table (device, n entries): the
+ * indices 0..n-1 grouped by key, ascending within each key; offsets (device,
+ * buckets+1 entries): offsets[k] = number of entries with a key below k, and
+ * offsets[buckets] = n.  The same table pt_setup builds for workplaces.
+ * n <= PT_STATIC_TABLE_MAX_ENTRIES and buckets <= PT_STATIC_TABLE_MAX_BUCKETS, else
+ * PT_ERR_ARG; a key outside [0, buckets) also gives PT_ERR_ARG.  Work runs on
+ * cuda_stream (NULL: the default stream) and the call returns once the table is
+ * complete.  The first call on a device looks up the scratch's device address; make
+ * that first call before any stream capture.  All calls share one scratch area, so
+ * calls that overlap on the GPU race with each other: do not overlap them. */
+pt_status pt_bucket_table_static(const int32_t *keys, int n, int buckets, int32_t *offsets,
+                                 int32_t *table, void *cuda_stream);
+
 void pt_destroy(pt_sim *sim);
 
 /* Text of the last error on sim (or of the last failed pt_create when sim is NULL). */

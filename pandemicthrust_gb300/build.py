@@ -20,7 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB = os.path.join(OUT, "libpandemic_gb300.so")
 CLI = os.path.join(OUT, "pt_sim")
 
-CUDA_SOURCES = ["pt_kernels.cu"]
+CUDA_SOURCES = ["pt_kernels.cu", "pt_static_table.cu"]
 HOST_SOURCES = ["pt_sim.cpp", "pt_host.cpp"]
 
 
