@@ -49,16 +49,17 @@ FALLBACK_HBM_GBS = 6800.0
 #   sweep     4N read (status + day, both strains) + 4I written (infected list)
 #   schedule  weekday 1N age read + 4E keys written; weekend 4E keys written
 #   scan      4Bc counts read + 4(Bc+1) offsets written
-#   sort      4E schedule read + 4E bucket table written
+#   sort      4E schedule read + 4E' bucket entries written, E' = entries of the
+#             buckets that the day's infected visit (the only ones materialised)
 #   infect    79 B per infected weekday, 52 B weekend
 #   apply     claim 8 B read + 8 B reset + state 4 B + generation 1 B per new infection
-def stage_bytes(stage, weekend, N, Bc, I_mean, new_mean=0.0):
+def stage_bytes(stage, weekend, N, Bc, I_mean, new_mean=0.0, mat_frac=1.0):
     E = (3 if weekend else 2) * N
     return {
         "sweep": 4 * N + 4 * I_mean,
         "schedule": (4 * E) if weekend else (N + 4 * E),
         "bucket_scan": 8 * Bc,
-        "bucket_sort": 8 * E,
+        "bucket_sort": 4 * E + 4 * E * mat_frac,
         "infect": (52 if weekend else 79) * I_mean,
         "apply": 21 * new_mean,
     }[stage]
@@ -283,6 +284,8 @@ def main():
     counts, infected = sim.runToCompletion()
     stages, (nwd, nwe) = sim.stage_ms()
     sim.set_timing(False)
+    tinfo = sim.info()
+    mat_frac = tinfo["bucket_entries_materialised"] / max(tinfo["bucket_entries_scheduled"], 1)
     days = len(infected)
     I_wd = [int(infected[d]) for d in range(days) if d % 7 < 5]
     I_we = [int(infected[d]) for d in range(days) if d % 7 >= 5]
@@ -296,15 +299,15 @@ def main():
     breakdown = {}
     for name in pt.PandemicSim.STAGES:
         tot = stages["weekday"][name] + stages["weekend"][name]
-        byt = (stage_bytes(name, False, N, Bc_wd, Imean_wd, new_wd) * nwd +
-               stage_bytes(name, True, N, Bc_we, Imean_we, new_we) * nwe)
+        byt = (stage_bytes(name, False, N, Bc_wd, Imean_wd, new_wd, mat_frac) * nwd +
+               stage_bytes(name, True, N, Bc_we, Imean_we, new_we, mat_frac) * nwe)
         breakdown[name] = {"ms": round(tot, 3), "share": round(tot / run_ms, 4) if run_ms else None,
                            "GBps": round(byt / (tot / 1000.0) / 1e9, 1) if tot > 0 else None}
     dominant = max(pt.PandemicSim.STAGES, key=lambda n: stages["weekday"][n] + stages["weekend"][n])
     dom_ms = stages["weekday"][dominant] + stages["weekend"][dominant]
     dom_launches = nwd + nwe
-    dom_bytes = (stage_bytes(dominant, False, N, Bc_wd, Imean_wd, new_wd) * nwd +
-                 stage_bytes(dominant, True, N, Bc_we, Imean_we, new_we) * nwe) / max(dom_launches, 1)
+    dom_bytes = (stage_bytes(dominant, False, N, Bc_wd, Imean_wd, new_wd, mat_frac) * nwd +
+                 stage_bytes(dominant, True, N, Bc_we, Imean_we, new_we, mat_frac) * nwe) / max(dom_launches, 1)
     achieved = dom_bytes / (dom_ms / dom_launches / 1000.0) / 1e9
     peak, peak_kind = measured_peaks()
     traffic = ncu_traffic().get(dominant)
@@ -365,6 +368,7 @@ def main():
             "day_roofline": {"achieved": day_achieved, "peak": peak, "unit": "GB/s", "frac": day_achieved / peak,
                              "bytes_per_run": all_bytes},
             "stages": breakdown,
+            "buckets_materialised_fraction": round(mat_frac, 4),
             "cpu_baseline": cpu,
             "clocks": clocks,
         }

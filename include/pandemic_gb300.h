@@ -66,6 +66,8 @@ typedef struct pt_info {
     float max_infected_proportion;
     int sm_count;
     uint64_t device_bytes;       /* device memory held by this simulation */
+    uint64_t bucket_entries_scheduled;    /* errand entries scheduled over the days run */
+    uint64_t bucket_entries_materialised; /* of those, entries written to bucket tables */
 } pt_info;
 
 typedef struct pt_sim pt_sim;
@@ -126,9 +128,17 @@ pt_status pt_get_population(pt_sim *sim, int32_t *household, int32_t *household_
 
 /* Copies the last built day's tables: infected list (infected_count entries),
  * schedule keys and bucketed person ids (2N weekday / 3N weekend) and bucket
- * offsets (2L+1 / 10L+1).  entries and buckets receive the sizes. */
+ * offsets (2L+1 / 10L+1), in the reference's layout (key = hour * L + location).
+ * entries and buckets receive the sizes.  By default a day materialises only the
+ * buckets that its infected persons visit (the only ones the contact draws read), so
+ * the person table is complete only after pt_set_full_tables(sim, 1). */
 pt_status pt_get_day_tables(pt_sim *sim, int32_t *infected, int32_t *keys, int32_t *people,
                             int32_t *offsets, int *entries, int *buckets);
+
+/* With enabled != 0 every day materialises all of its buckets, not only those its
+ * infected persons visit.  Results are identical either way; this exists so the
+ * tables returned by pt_get_day_tables are complete. */
+pt_status pt_set_full_tables(pt_sim *sim, int enabled);
 
 /* Device time per stage, from CUDA events recorded on the simulation's stream
  * around each stage of every day run while timing is enabled (pt_set_timing).

@@ -63,14 +63,15 @@ class Info(ctypes.Structure):
         ("type_count", ctypes.c_int * 14), ("type_offset", ctypes.c_int * 14),
         ("infectiousness", ctypes.c_float * 2), ("max_day_of_peak", ctypes.c_int),
         ("max_infected_proportion", ctypes.c_float), ("sm_count", ctypes.c_int),
-        ("device_bytes", ctypes.c_uint64),
+        ("device_bytes", ctypes.c_uint64), ("bucket_entries_scheduled", ctypes.c_uint64),
+        ("bucket_entries_materialised", ctypes.c_uint64),
     ]
 
 
 EXPORTS = [
     "pt_params_from_csv", "pt_seed_from_file", "pt_create", "pt_setup", "pt_step_day", "pt_run",
     "pt_final_gen_counts", "pt_reset_epidemic", "pt_get_info", "pt_get_person_state",
-    "pt_get_population", "pt_get_day_tables", "pt_set_timing", "pt_get_stage_ms",
+    "pt_get_population", "pt_get_day_tables", "pt_set_full_tables", "pt_set_timing", "pt_get_stage_ms",
     "pt_launch_count", "pt_transfer_bytes", "pt_destroy", "pt_last_error",
 ]
 
@@ -105,6 +106,7 @@ def load_library(path=None):
     lib.pt_get_population.argtypes = [vp] + [i32p] * 5
     lib.pt_get_day_tables.argtypes = [vp, i32p, i32p, i32p, i32p, ip, ip]
     lib.pt_set_timing.argtypes = [vp, ctypes.c_int]
+    lib.pt_set_full_tables.argtypes = [vp, ctypes.c_int]
     lib.pt_get_stage_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ip]
     lib.pt_launch_count.restype = ctypes.c_uint64
     lib.pt_launch_count.argtypes = []
@@ -207,6 +209,10 @@ class PandemicSim:
                                                ctypes.byref(e), ctypes.byref(b)))
         return dict(infected=infected, keys=keys[:e.value], people=people[:e.value],
                     offsets=offsets[:b.value + 1], entries=e.value, buckets=b.value)
+
+    def set_full_tables(self, on=True):
+        """Materialise every bucket each day (complete tables for day_tables())."""
+        self._check(self.lib.pt_set_full_tables(self.h, 1 if on else 0))
 
     def set_timing(self, on=True):
         self._check(self.lib.pt_set_timing(self.h, 1 if on else 0))

@@ -200,7 +200,9 @@ constexpr int kScanThreads = 256, kScanItems = 16, kScanTile = kScanThreads * kS
 constexpr int kMaxRadixPasses = 4;
 
 __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *in, int32_t *out, int n, int clear_in,
-                                                       LookBack lb, const int *skip, int passes, int *digit_hist)
+                                                       LookBack lb, const int *skip, int passes, int *digit_hist,
+                                                       const uint32_t *mark, int *total_out,
+                                                       unsigned long long *total_accum)
 {
     if (skip && *(volatile const int *)skip) return;
     __shared__ int s_dh[kMaxRadixPasses][256];
@@ -217,6 +219,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *in, int32_
     for (int k = 0; k < kScanItems; k++) {
         long long i = base + k;
         v[k] = i < n ? in[i] : 0;
+        // with a mark filter only marked buckets keep their entries
+        if (mark && i < n && !((mark[i >> 5] >> (i & 31)) & 1u)) v[k] = 0;
         sum += v[k];
     }
     if (clear_in) {
@@ -247,7 +251,11 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *in, int32_
         if (i < n) out[i] = run;
         run += v[k];
     }
-    if (tile == (int)gridDim.x - 1 && threadIdx.x == 0) out[n] = (int)s_prefix + total;
+    if (tile == (int)gridDim.x - 1 && threadIdx.x == 0) {
+        out[n] = (int)s_prefix + total;
+        if (total_out) *total_out = (int)s_prefix + total;
+        if (total_accum) *total_accum += (unsigned long long)((int)s_prefix + total);
+    }
     if (passes > 0) {
         for (int p = 0; p < passes; p++) {
             int c = s_dh[p][threadIdx.x];
@@ -269,14 +277,16 @@ static LookBack make_lb(unsigned long long *tiles, int tiles_cap, int *error)
 
 cudaError_t launch_scan_exclusive(const int32_t *in, int32_t *out, int n, int clear_in,
                                   unsigned long long *tiles, int *ctl, int *error,
-                                  const int *skip, int passes, int *digit_hist, cudaStream_t s)
+                                  const int *skip, int passes, int *digit_hist, cudaStream_t s,
+                                  const uint32_t *mark, int *total_out, unsigned long long *total_accum)
 {
     int blocks = std::max(1, div_up(n, kScanTile));
     LookBack lb;
     lb.tiles = tiles;
     lb.ctl = ctl;
     lb.error = error;
-    k_scan<<<blocks, kScanThreads, 0, s>>>(in, out, n, clear_in, lb, skip, passes, digit_hist);
+    k_scan<<<blocks, kScanThreads, 0, s>>>(in, out, n, clear_in, lb, skip, passes, digit_hist, mark, total_out,
+                                                           total_accum);
     count_launch();
     return cudaGetLastError();
 }
@@ -406,14 +416,27 @@ __device__ __forceinline__ unsigned digit_peers(unsigned d, int nbits, unsigned 
     return peers;
 }
 
+// Per-item rank record kept between the two phases of a pass:
+// bits 0-7 digit, 8-12 rank among same-digit lanes of the warp round, 13-18 their
+// count, bit 19 valid.
+__device__ __forceinline__ uint32_t pack_rank(unsigned d, unsigned rank, unsigned cnt, bool ok)
+{
+    return d | (rank << 8) | (cnt << 13) | ((unsigned)ok << 19);
+}
+
+// One stable radix pass over 8 bits of the keys.  FILTER (first pass only) drops
+// entries whose bucket is not set in `mark`; passes after a filtered first pass read
+// their entry count from *count_dev.
 template <int MODE>
 __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t *__restrict__ keys_in,
-                                                              const uint32_t *__restrict__ vals_in,
-                                                              uint32_t *__restrict__ keys_out,
-                                                              uint32_t *__restrict__ vals_out, int E, int shift,
-                                                              int nbits, int N, int person_mode,
-                                                              const int *__restrict__ digit_base,
-                                                              uint32_t *status, int *ctl, int *error, const int *skip)
+                                                                 const uint32_t *__restrict__ vals_in,
+                                                                 uint32_t *__restrict__ keys_out,
+                                                                 uint32_t *__restrict__ vals_out, int E_arg,
+                                                                 const int *count_dev, const uint32_t *mark,
+                                                                 int shift, int nbits, int N, int person_mode,
+                                                                 const int *__restrict__ digit_base,
+                                                                 uint32_t *status, int *ctl, int *error,
+                                                                 const int *skip)
 {
     if (skip && *(volatile const int *)skip) return;
     __shared__ int s_tile;
@@ -423,79 +446,93 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
     for (int i = threadIdx.x; i < kRadixWarps * 256; i += kRadixThreads) (&s_hist[0][0])[i] = 0;
     __syncthreads();
     const int tile = s_tile;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const unsigned lt = (1u << lane) - 1u;
-    const long long base = (long long)tile * kRadixTile + (long long)warp * kRadixWarpItems + lane;
-    uint32_t key[kRadixItems], val[kRadixItems];
+    const int E = count_dev ? *(volatile const int *)count_dev : E_arg;
+    if (tile * kRadixTile < E) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const unsigned lt = (1u << lane) - 1u;
+        const int base = tile * kRadixTile + warp * kRadixWarpItems + lane;
+        const bool full = (tile + 1) * kRadixTile <= E;
+        uint32_t key[kRadixItems], val[kRadixItems], info[kRadixItems];
 #pragma unroll
-    for (int j = 0; j < kRadixItems; j++) {
-        const long long i = base + 32 * j;
-        const bool ok = i < E;
-        key[j] = ok ? keys_in[i] : 0u;
-        if (MODE == kRadixFirst || MODE == kRadixOnly) val[j] = entry_person(i, N, person_mode);
-        else val[j] = ok ? vals_in[i] : 0u;
-    }
-    // per-warp digit counts (each warp owns one row; its rounds run in order)
-#pragma unroll
-    for (int j = 0; j < kRadixItems; j++) {
-        const bool ok = base + 32 * j < E;
-        const unsigned d = (key[j] >> shift) & 255u;
-        const unsigned peers = digit_peers(d, nbits, __ballot_sync(0xffffffffu, ok));
-        if (ok && (peers & lt) == 0) s_hist[warp][d] += __popc(peers);
-    }
-    __syncthreads();
-    {
-        // thread d: exclusive bases of the warps for digit d, then the look-back
-        const int d = threadIdx.x;
-        int run = 0;
-#pragma unroll
-        for (int w = 0; w < kRadixWarps; w++) {
-            int c = s_hist[w][d];
-            s_hist[w][d] = run;
-            run += c;
-        }
-        volatile uint32_t *st = status;
-        int excl = 0;
-        if (tile == 0) {
-            st[d] = (2u << 30) | (uint32_t)run;
-        } else {
-            st[(size_t)tile * 256 + d] = (1u << 30) | (uint32_t)run;
-            int t = tile - 1;
-            long long spins = 0;
-            while (t >= 0) {
-                const uint32_t w = st[(size_t)t * 256 + d];
-                const uint32_t flag = w >> 30;
-                if (flag == 0) {
-                    if (++spins > kSpinLimit) {
-                        atomicExch(error, 2);
-                        break;
-                    }
-                    __nanosleep(32);
-                    continue;
-                }
-                excl += (int)(w & 0x3FFFFFFFu);
-                if (flag == 2) break;
-                t--;
+        for (int j = 0; j < kRadixItems; j++) {
+            const int i = base + 32 * j;
+            const bool in = full || i < E;
+            key[j] = in ? keys_in[i] : 0u;
+            if (MODE == kRadixFirst || MODE == kRadixOnly) {
+                const uint32_t u = (uint32_t)i;
+                val[j] = person_mode == 0 ? u : (person_mode == 1 ? (u < (uint32_t)N ? u : u - (uint32_t)N) : u / 3u);
+            } else {
+                val[j] = in ? vals_in[i] : 0u;
             }
-            st[(size_t)tile * 256 + d] = (2u << 30) | (uint32_t)(excl + run);
         }
-        s_base[d] = digit_base[d] + excl;
-    }
-    __syncthreads();
+        // phase A: rank within the warp round, per-warp digit counts
 #pragma unroll
-    for (int j = 0; j < kRadixItems; j++) {
-        const bool ok = base + 32 * j < E;
-        const unsigned d = (key[j] >> shift) & 255u;
-        const unsigned peers = digit_peers(d, nbits, __ballot_sync(0xffffffffu, ok));
-        const int wbase = ok ? s_hist[warp][d] : 0;
-        __syncwarp();
-        if (ok) {
-            const int pos = s_base[d] + wbase + __popc(peers & lt);
-            if (MODE == kRadixFirst || MODE == kRadixMiddle) keys_out[pos] = key[j];
-            vals_out[pos] = val[j];
-            if ((peers & lt) == 0) s_hist[warp][d] = wbase + __popc(peers);
+        for (int j = 0; j < kRadixItems; j++) {
+            const int i = base + 32 * j;
+            bool ok = full || i < E;
+            if ((MODE == kRadixFirst || MODE == kRadixOnly) && mark && ok)
+                ok = (mark[key[j] >> 5] >> (key[j] & 31u)) & 1u;
+            const unsigned d = (key[j] >> shift) & 255u;
+            const unsigned peers = digit_peers(d, nbits, __ballot_sync(0xffffffffu, ok));
+            const unsigned rank = __popc(peers & lt), cnt = __popc(peers);
+            if (ok && rank == 0) s_hist[warp][d] += cnt;
+            info[j] = pack_rank(d, rank, cnt, ok);
         }
-        __syncwarp();
+        __syncthreads();
+        {
+            // thread d: exclusive bases of the warps for digit d, then the look-back
+            const int d = threadIdx.x;
+            int run = 0;
+#pragma unroll
+            for (int w = 0; w < kRadixWarps; w++) {
+                int c = s_hist[w][d];
+                s_hist[w][d] = run;
+                run += c;
+            }
+            volatile uint32_t *st = status;
+            int excl = 0;
+            if (tile == 0) {
+                st[d] = (2u << 30) | (uint32_t)run;
+            } else {
+                st[(size_t)tile * 256 + d] = (1u << 30) | (uint32_t)run;
+                int t = tile - 1;
+                long long spins = 0;
+                while (t >= 0) {
+                    const uint32_t w = st[(size_t)t * 256 + d];
+                    const uint32_t flag = w >> 30;
+                    if (flag == 0) {
+                        if (++spins > kSpinLimit) {
+                            atomicExch(error, 2);
+                            break;
+                        }
+                        __nanosleep(32);
+                        continue;
+                    }
+                    excl += (int)(w & 0x3FFFFFFFu);
+                    if (flag == 2) break;
+                    t--;
+                }
+                st[(size_t)tile * 256 + d] = (2u << 30) | (uint32_t)(excl + run);
+            }
+            s_base[d] = digit_base[d] + excl;
+        }
+        __syncthreads();
+        // phase B: write each entry at its global position
+#pragma unroll
+        for (int j = 0; j < kRadixItems; j++) {
+            const uint32_t r = info[j];
+            const bool ok = (r >> 19) & 1u;
+            const unsigned d = r & 255u, rank = (r >> 8) & 31u, cnt = (r >> 13) & 63u;
+            const int wbase = ok ? s_hist[warp][d] : 0;
+            __syncwarp();
+            if (ok) {
+                const int pos = s_base[d] + wbase + (int)rank;
+                if (MODE == kRadixFirst || MODE == kRadixMiddle) keys_out[pos] = key[j];
+                vals_out[pos] = val[j];
+                if (rank == 0) s_hist[warp][d] = wbase + (int)cnt;
+            }
+            __syncwarp();
+        }
     }
     if (threadIdx.x == 0) {
         __threadfence();
@@ -532,18 +569,19 @@ cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
         const int *db = r.digit_base + 256 * p;
         const int shift = 8 * p;
         const int nbits = std::max(1, std::min(8, bits - shift));
+        // the first pass reads all E entries (and filters); later ones the survivors
+        const int *cnt = (p == 0) ? nullptr : r.count_dev;
+        const uint32_t *mk = (p == 0) ? r.mark : nullptr;
+#define PT_RADIX_ARGS kin, vin, kout, vout, r.E, cnt, mk, shift, nbits, r.N, r.person_mode, db, r.status, r.ctl, r.error, r.skip
         if (P == 1)
-            k_radix_pass<kRadixOnly><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, nbits, r.N,
-                                                                    r.person_mode, db, r.status, r.ctl, r.error, r.skip);
+            k_radix_pass<kRadixOnly><<<tiles, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
         else if (p == 0)
-            k_radix_pass<kRadixFirst><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, nbits, r.N,
-                                                                     r.person_mode, db, r.status, r.ctl, r.error, r.skip);
+            k_radix_pass<kRadixFirst><<<tiles, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
         else if (p == P - 1)
-            k_radix_pass<kRadixLast><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, nbits, r.N,
-                                                                    r.person_mode, db, r.status, r.ctl, r.error, r.skip);
+            k_radix_pass<kRadixLast><<<tiles, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
         else
-            k_radix_pass<kRadixMiddle><<<tiles, kRadixThreads, 0, s>>>(kin, vin, kout, vout, r.E, shift, nbits, r.N,
-                                                                      r.person_mode, db, r.status, r.ctl, r.error, r.skip);
+            k_radix_pass<kRadixMiddle><<<tiles, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+#undef PT_RADIX_ARGS
         count_launch();
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
@@ -564,7 +602,7 @@ cudaError_t launch_bucket_table(const RadixArgs &r, int32_t *counts, bool count_
         if (e != cudaSuccess) return e;
     }
     cudaError_t e = launch_scan_exclusive(counts, offset, r.buckets, 1, tiles, lb_ctl, r.error, r.skip, P,
-                                          digit_hist, s);
+                                          digit_hist, s, nullptr, nullptr);
     if (e != cudaSuccess) return e;
     k_digit_bases<<<1, 256, 0, s>>>(digit_hist, (int *)r.digit_base, P, r.skip);
     count_launch();
@@ -843,6 +881,8 @@ static RadixArgs day_radix_args(const SimConst &c, const DevArrays &d, bool week
     r.buckets = day_buckets(c, weekend);
     r.N = c.N;
     r.person_mode = weekend ? 2 : 1;
+    r.mark = d.mark;
+    r.count_dev = &d.sc->marked_entries;
     r.k0 = d.rk0; r.v0 = d.rv0; r.k1 = d.rk1; r.v1 = d.rv1;
     r.out = (uint32_t *)d.bkt_people;
     r.digit_base = d.digit_base;
@@ -853,13 +893,40 @@ static RadixArgs day_radix_args(const SimConst &c, const DevArrays &d, bool week
     return r;
 }
 
-cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s)
+// Marks the errand buckets of today's infected: the only buckets the infection
+// kernels sample.  Every bucket of an infected person is marked (a superset of the
+// ones its contact profile uses).
+__global__ void k_mark_buckets(const int32_t *keys, const int32_t *infected, int N, int weekend, uint32_t *mark,
+                               const Scalars *sc)
+{
+    if (sc->done) return;
+    const int I = sc->infected;
+    const int per = weekend ? 3 : 2;
+    for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < I; pos += gridDim.x * blockDim.x) {
+        const int me = infected[pos];
+        for (int k = 0; k < per; k++) {
+            const int b = weekend ? keys[3 * (size_t)me + k] : keys[(size_t)k * N + me];
+            atomicOr(&mark[b >> 5], 1u << (b & 31));
+        }
+    }
+}
+
+cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weekend, bool full_tables, cudaStream_t s)
 {
     RadixArgs r = day_radix_args(c, d, weekend);
     const int P = radix_passes(r.buckets);
-    cudaError_t e = launch_scan_exclusive(d.bkt_count, d.bkt_offset, r.buckets, 1, d.tiles,
-                                          (int *)(d.tiles + d.tiles_cap), &d.sc->error, &d.sc->done, P,
-                                          d.digit_hist, s);
+    const size_t mark_bytes = ((size_t)r.buckets / 32 + 1) * 4;
+    cudaError_t e = cudaMemsetAsync(d.mark, full_tables ? 0xFF : 0, mark_bytes, s);
+    if (e != cudaSuccess) return e;
+    if (!full_tables) {
+        k_mark_buckets<<<sm_count() * 4, 256, 0, s>>>(d.keys, d.infected, c.N, weekend ? 1 : 0, d.mark, d.sc);
+        count_launch();
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    e = launch_scan_exclusive(d.bkt_count, d.bkt_offset, r.buckets, 1, d.tiles, (int *)(d.tiles + d.tiles_cap),
+                              &d.sc->error, &d.sc->done, P, d.digit_hist, s, d.mark, &d.sc->marked_entries,
+                              &d.sc->materialised_sum);
     if (e != cudaSuccess) return e;
     k_digit_bases<<<1, 256, 0, s>>>(d.digit_hist, d.digit_base, P, &d.sc->done);
     count_launch();

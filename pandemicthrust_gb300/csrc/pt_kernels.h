@@ -27,6 +27,7 @@ struct SimConst {
 // these on the device, so a whole run needs no host round trip.
 struct Scalars {
     unsigned long long rand_offset;     // next free Random123 counter
+    unsigned long long materialised_sum;  // schedule entries written to bucket tables, all days
     unsigned long long errand_offset;   // E0 of the current day's schedule
     unsigned long long infect_offset;   // R0 of the current day's contacts
     int infected;                       // infected count of the current day
@@ -38,8 +39,8 @@ struct Scalars {
     int tile_ticket2;
     int error;                          // nonzero: a bounded device wait gave up
     int error_site;
-    int mid_count;                      // buckets for the warp sort
-    int big_count;                      // buckets for the block sort
+    int marked_entries;                 // schedule entries in today's materialised buckets
+    int unused;
     int adults;
     int pad[2];
     int counts[kMaxDays][16];           // per-day status bins
@@ -65,6 +66,7 @@ struct DevArrays {
     int *radix_ctl;           // ticket, finished
     int *digit_hist;          // 4 x 256
     int *digit_base;          // 4 x 256
+    uint32_t *mark;           // bitmap over today's buckets: 1 = materialise
     int32_t *infected;        // N ascending infected ids
     unsigned long long *claim;// 2N (victim, strain) -> min attempt key
     int32_t *new_list;        // 2N first claims of the day
@@ -81,7 +83,9 @@ cudaError_t launch_household_types(const SimConst &c, uint8_t *types, int32_t *s
                                    cudaStream_t s);
 cudaError_t launch_scan_exclusive(const int32_t *in, int32_t *out, int n, int clear_in,
                                   unsigned long long *tiles, int *ctl, int *error,
-                                  const int *skip, int passes, int *digit_hist, cudaStream_t s);
+                                  const int *skip, int passes, int *digit_hist, cudaStream_t s,
+                                  const uint32_t *mark = nullptr, int *total_out = nullptr,
+                                  unsigned long long *total_accum = nullptr);
 cudaError_t launch_generate_households(const SimConst &c, const uint8_t *types, const int32_t *hh_offset,
                                        int32_t *household, uint8_t *age, cudaStream_t s);
 cudaError_t launch_assign_workplaces(const SimConst &c, uint8_t *age, int32_t *workplace, cudaStream_t s);
@@ -92,6 +96,8 @@ cudaError_t launch_count_keys(const int32_t *keys, int n, int32_t *count, cudaSt
 struct RadixArgs {
     const uint32_t *keys;
     int E, buckets, N, person_mode;
+    const uint32_t *mark = nullptr;   // optional bucket filter of the first pass
+    const int *count_dev = nullptr;   // entry count after the filter (device)
     uint32_t *k0, *v0, *k1, *v1, *out;
     const int *digit_base;
     uint32_t *status;
@@ -113,7 +119,7 @@ cudaError_t launch_seed_infected(const int32_t *seeds, int P, int S, uint32_t *s
 cudaError_t launch_sweep(const SimConst &c, const DevArrays &d, int day, cudaStream_t s);
 cudaError_t launch_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
 int day_buckets(const SimConst &c, bool weekend);
-cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
+cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weekend, bool full_tables, cudaStream_t s);
 cudaError_t launch_bucket_sort(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
 cudaError_t launch_infect(const SimConst &c, const DevArrays &d, bool weekend, int day, cudaStream_t s);
 cudaError_t launch_apply(const DevArrays &d, int day, cudaStream_t s);

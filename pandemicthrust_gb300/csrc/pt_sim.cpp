@@ -59,6 +59,7 @@ struct pt_sim {
     int days_run = 0;
     std::string err;
     bool timing = false;
+    bool full_tables = false;             // materialise every bucket (tables complete for inspection)
     std::vector<cudaEvent_t> day_events;  // kMaxDays x (stages + 1), created on demand
     std::vector<int> timed_days;
     float stage_ms[16] = {0};             // [weekday stages 0..7, weekend stages 8..15]
@@ -244,6 +245,7 @@ pt_status pt_setup(pt_sim *s)
     bytes += round256(B * 4);                 // bkt_count
     bytes += round256(radix_tiles * 256 * 4); // radix look-back words
     bytes += round256(8 * 4) + 2 * round256(4 * 256 * 4);  // radix ctl, digit hist/base
+    bytes += round256((B / 32 + 1) * 4);      // bucket mark bitmap
     bytes += round256(n * 4);                 // infected
     bytes += round256(2 * n * 8);             // claim
     bytes += round256(2 * n * 4);             // new_list
@@ -271,6 +273,7 @@ pt_status pt_setup(pt_sim *s)
     d.radix_ctl = a.take<int>(8);
     d.digit_hist = a.take<int>(4 * 256);
     d.digit_base = a.take<int>(4 * 256);
+    d.mark = a.take<uint32_t>(B / 32 + 1);
     d.infected = a.take<int32_t>(n);
     d.claim = a.take<unsigned long long>(2 * n);
     d.new_list = a.take<int32_t>(2 * n);
@@ -345,7 +348,7 @@ static pt_status enqueue_day(pt_sim *s, int day)
     if (t) cudaEventRecord(stage_event(s, day, 1), st);
     CK(ptk::launch_schedule(c, d, weekend, st), "schedule");
     if (t) cudaEventRecord(stage_event(s, day, 2), st);
-    CK(ptk::launch_bucket_scan(c, d, weekend, st), "bucket scan");
+    CK(ptk::launch_bucket_scan(c, d, weekend, s->full_tables, st), "bucket scan");
     if (t) cudaEventRecord(stage_event(s, day, 3), st);
     CK(ptk::launch_bucket_sort(c, d, weekend, st), "bucket sort");
     if (t) cudaEventRecord(stage_event(s, day, 4), st);
@@ -523,9 +526,14 @@ pt_status pt_get_info(const pt_sim *s, pt_info *out)
     out->sm_count = ptk::sm_count();
     out->device_bytes = s->arena_bytes + s->small_bytes;
     if (s->setup_done) {
-        unsigned long long ro = 0;
-        pt_memcpy_sync(s, &ro, &s->d.sc->rand_offset, sizeof(ro), cudaMemcpyDeviceToHost);
-        out->rand_offset = ro;
+        unsigned long long v[2] = {0, 0};
+        pt_memcpy_sync(s, v, &s->d.sc->rand_offset, sizeof(v), cudaMemcpyDeviceToHost);
+        out->rand_offset = v[0];
+        out->bucket_entries_materialised = v[1];
+        uint64_t total = 0;
+        for (int day = 0; day < s->days_run; day++)
+            if (s->infected[day] > 0) total += (uint64_t)((day % 7) >= 5 ? 3 : 2) * (uint64_t)s->c.N;
+        out->bucket_entries_scheduled = total;
     }
     return PT_OK;
 }
@@ -610,6 +618,19 @@ pt_status pt_get_day_tables(pt_sim *s, int32_t *infected, int32_t *keys, int32_t
                 offsets[(size_t)h * L + loc] = loc < lo ? co[(size_t)h * R] : co[(size_t)h * R + loc - lo];
         offsets[B] = E;
     }
+    return PT_OK;
+}
+
+pt_status pt_set_full_tables(pt_sim *s, int enabled)
+{
+    if (!s) return PT_ERR_ARG;
+    const bool v = enabled != 0;
+    if (v != s->full_tables && s->run_graph) {
+        // the captured day loop bakes this choice in; capture again on the next run
+        cudaGraphExecDestroy(s->run_graph);
+        s->run_graph = nullptr;
+    }
+    s->full_tables = v;
     return PT_OK;
 }
 

@@ -77,6 +77,7 @@ def test_setup_matches_oracle(native_lib, oracle_built):
 
 def test_config1_days_match_oracle_stage_by_stage(native_lib, oracle_built):
     sim = pt.PandemicSim(C1, 12345)
+    sim.set_full_tables(True)
     sim.setupSim()
     o = Oracle(C1, 12345)
     o.setup()
@@ -138,6 +139,27 @@ def test_run_on_device_equals_day_steps(native_lib):
     b.close()
 
 
+def test_lazy_buckets_equal_full_tables(native_lib):
+    # materialising only the buckets infected persons visit must not change anything
+    p = make_params(max_days=60, people_scaling=0.1, location_scaling=0.1, percent_symptomatic=0.8,
+                    asymp_factor=0.2)
+    runs = []
+    for full in (False, True):
+        sim = pt.PandemicSim(p, 31)
+        sim.set_full_tables(full)
+        sim.setupSim()
+        counts, infected = sim.runToCompletion()
+        info = sim.info()
+        runs.append((counts, infected, sim.person_state(), info))
+        sim.close()
+    (c0, i0, s0, f0), (c1, i1, s1, f1) = runs
+    assert np.array_equal(c0, c1) and np.array_equal(i0, i1)
+    for k in s0:
+        assert np.array_equal(s0[k], s1[k]), k
+    assert f1["bucket_entries_materialised"] == f1["bucket_entries_scheduled"]
+    assert f0["bucket_entries_materialised"] < f0["bucket_entries_scheduled"]
+
+
 def test_deterministic_and_resettable(native_lib):
     p = make_params(max_days=25, people_scaling=0.08, location_scaling=0.02)
     sim = pt.PandemicSim(p, 5)
@@ -158,6 +180,7 @@ def test_config2_shape_one_million_matches_oracle(native_lib, oracle_built):
     p = make_params(max_days=21, r_pandemic=1.5, r_seasonal=1.2, initial_pandemic=100, initial_seasonal=100,
                     people_scaling=0.42481, location_scaling=4.2481)
     sim = pt.PandemicSim(p, 777)
+    sim.set_full_tables(True)
     sim.setupSim()
     o = Oracle(p, 777, threads=8)
     o.setup()
