@@ -560,7 +560,8 @@ cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
     const int bits = key_bits(r.buckets);
     const int tiles = std::max(1, div_up(r.E, kRadixTile));
     const uint32_t *kin = r.keys;
-    const uint32_t *vin = nullptr;
+    const uint32_t *vin = r.vals;   // nullptr: implicit values (entry index -> person)
+    const bool implicit = r.vals == nullptr;
     for (int p = 0; p < P; p++) {
         cudaError_t e = cudaMemsetAsync(r.status, 0, (size_t)tiles * 256 * sizeof(uint32_t), s);
         if (e != cudaSuccess) return e;
@@ -569,13 +570,14 @@ cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
         const int *db = r.digit_base + 256 * p;
         const int shift = 8 * p;
         const int nbits = std::max(1, std::min(8, bits - shift));
-        // the first pass reads all E entries (and filters); later ones the survivors
-        const int *cnt = (p == 0) ? nullptr : r.count_dev;
+        // the first pass of an implicit-value sort reads all E entries (and may
+        // filter); every other pass reads the count on the device, if any
+        const int *cnt = (p == 0 && implicit) ? nullptr : r.count_dev;
         const uint32_t *mk = (p == 0) ? r.mark : nullptr;
 #define PT_RADIX_ARGS kin, vin, kout, vout, r.E, cnt, mk, shift, nbits, r.N, r.person_mode, db, r.status, r.ctl, r.error, r.skip
-        if (P == 1)
+        if (P == 1 && implicit)
             k_radix_pass<kRadixOnly><<<tiles, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
-        else if (p == 0)
+        else if (p == 0 && implicit)
             k_radix_pass<kRadixFirst><<<tiles, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
         else if (p == P - 1)
             k_radix_pass<kRadixLast><<<tiles, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
@@ -804,55 +806,153 @@ cudaError_t launch_sweep(const SimConst &c, const DevArrays &d, int day, cudaStr
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ schedules
 // Weekday schedule (kernel_assignWeekdayAfterschoolAndErrands, PandemicSim.cu:2972-3022):
 // counter E0 + g -> persons 2g, 2g+1.  Hour-0 keys at [0,N), hour-1 keys at [N,2N).
 // Weekday destinations lie in [lo, L), lo = first location of type 8 (afterschool),
 // so the bucket index is hour * R + dest - lo with R = L - lo (order-preserving).
-__global__ void k_sched_weekday(SimConst c, const uint8_t *age, int32_t *keys, int32_t *count, const Scalars *sc)
+__device__ __forceinline__ void weekday_pair_keys(const SimConst &c, const uint32_t w[4], int k, bool adult, int lo,
+                                                  int R, int &k1, int &k2)
+{
+    int d1 = fish_weekday_dest(c, w[2 * k], adult);
+    int d2 = adult ? fish_weekday_dest(c, w[2 * k + 1], true) : d1;
+    k1 = d1 - lo;
+    k2 = R + d2 - lo;
+}
+
+__device__ __forceinline__ bool is_marked(const uint32_t *mark, int b) { return (mark[b >> 5] >> (b & 31)) & 1u; }
+
+// Marks the errand buckets of today's infected: the only buckets the contact draws
+// read.  Their destinations are regenerated from the schedule counter, as the
+// reference's device_recalc_* functions do (PandemicSim.cu:3667-3705, :3742-3746).
+// Every errand of an infected person is marked, a superset of the ones its contact
+// profile uses.
+__global__ void k_mark_buckets(SimConst c, const uint8_t *age, const int32_t *infected, int weekend, uint32_t *mark,
+                               const Scalars *sc)
 {
     if (sc->done) return;
     const TfKey key = make_key(c);
+    const int I = sc->infected;
     const unsigned long long E0 = sc->errand_offset;
-    const int N = c.N, G = N / 2;
-    const int lo = c.type_offset[8], R = c.L - lo;
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x) {
-        uint32_t w[4];
-        tf2x64(key, E0 + (uint64_t)g, w);
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-            int p = 2 * g + k;
-            if (p < N) {
-                bool adult = age[p] == 5;
-                int d1 = fish_weekday_dest(c, w[2 * k], adult);
-                int d2 = adult ? fish_weekday_dest(c, w[2 * k + 1], true) : d1;
-                const int k1 = d1 - lo, k2 = R + d2 - lo;
-                keys[p] = k1;
-                keys[N + p] = k2;
-                atomicAdd(&count[k1], 1);
-                atomicAdd(&count[k2], 1);
-            }
+    for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < I; pos += gridDim.x * blockDim.x) {
+        const int me = infected[pos];
+        if (weekend) {
+            const int lo = c.type_offset[9], R = c.L - lo;
+            int d[3];
+            weekend_errands(c, key, E0 + 2ull * (unsigned long long)me, lo, R, d);
+            for (int k = 0; k < 3; k++) atomicOr(&mark[d[k] >> 5], 1u << (d[k] & 31));
+        } else {
+            const int lo = c.type_offset[8], R = c.L - lo;
+            uint32_t w[4];
+            tf2x64(key, E0 + (uint64_t)(me / 2), w);
+            int k1, k2;
+            weekday_pair_keys(c, w, me & 1, age[me] == 5, lo, R, k1, k2);
+            atomicOr(&mark[k1 >> 5], 1u << (k1 & 31));
+            atomicOr(&mark[k2 >> 5], 1u << (k2 & 31));
         }
     }
 }
 
-// Weekend schedule (kernel_assignWeekendErrands, PandemicSim.cu:2082-2094): person p
-// uses counters E0 + 2p and E0 + 2p + 1; keys at [3p, 3p+3).
-__global__ void k_sched_weekend(SimConst c, int32_t *keys, int32_t *count, const Scalars *sc)
+// Schedule kernel, one tile of 4096 persons per block (16 contiguous persons per
+// thread).  It writes every person's keys, counts the entries of marked buckets and
+// appends those entries as (key, person) in ascending person order (block scan +
+// decoupled look-back), the order the radix sort needs for stability.
+constexpr int kSchedThreads = 256, kSchedPer = 16, kSchedTile = kSchedThreads * kSchedPer;
+
+template <bool WEEKEND>
+__global__ void __launch_bounds__(kSchedThreads) k_sched(SimConst c, const uint8_t *age, const uint32_t *mark,
+                                                         int32_t *keys, int32_t *count, uint32_t *ckeys,
+                                                         uint32_t *cvals, Scalars *sc, LookBack lb)
 {
-    if (sc->done) return;
+    if (*(volatile int *)&sc->done) return;
+    int tile;
+    unsigned epoch;
+    lookback_begin(lb, tile, epoch);
     const TfKey key = make_key(c);
     const unsigned long long E0 = sc->errand_offset;
-    const int lo = c.type_offset[9], R = c.L - lo;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < c.N; p += gridDim.x * blockDim.x) {
-        int d[3];
-        weekend_errands(c, key, E0 + 2ull * (unsigned long long)p, lo, R, d);
-        keys[3 * (size_t)p + 0] = d[0];
-        keys[3 * (size_t)p + 1] = d[1];
-        keys[3 * (size_t)p + 2] = d[2];
-        atomicAdd(&count[d[0]], 1);
-        atomicAdd(&count[d[1]], 1);
-        atomicAdd(&count[d[2]], 1);
+    const int N = c.N;
+    const int p0 = tile * kSchedTile + threadIdx.x * kSchedPer;
+    int mine = 0;
+    if (WEEKEND) {
+        // kernel_assignWeekendErrands (PandemicSim.cu:2082-2094): counters E0 + 2p, E0 + 2p + 1
+        const int lo = c.type_offset[9], R = c.L - lo;
+        for (int i = 0; i < kSchedPer; i++) {
+            const int p = p0 + i;
+            if (p >= N) break;
+            int d[3];
+            weekend_errands(c, key, E0 + 2ull * (unsigned long long)p, lo, R, d);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                keys[3 * (size_t)p + k] = d[k];
+                if (is_marked(mark, d[k])) {
+                    atomicAdd(&count[d[k]], 1);
+                    mine++;
+                }
+            }
+        }
+    } else {
+        const int lo = c.type_offset[8], R = c.L - lo;
+        for (int i = 0; i < kSchedPer; i += 2) {
+            const int p = p0 + i;  // even: counter E0 + p/2 covers persons p, p+1
+            if (p >= N) break;
+            uint32_t w[4];
+            tf2x64(key, E0 + (uint64_t)(p / 2), w);
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const int q = p + k;
+                if (q < N) {
+                    int k1, k2;
+                    weekday_pair_keys(c, w, k, age[q] == 5, lo, R, k1, k2);
+                    keys[q] = k1;
+                    keys[(size_t)N + q] = k2;
+                    if (is_marked(mark, k1)) {
+                        atomicAdd(&count[k1], 1);
+                        mine++;
+                    }
+                    if (is_marked(mark, k2)) {
+                        atomicAdd(&count[k2], 1);
+                        mine++;
+                    }
+                }
+            }
+        }
     }
+    int total;
+    const int excl = block_exclusive_scan<kSchedThreads, int>(mine, total);
+    __shared__ unsigned s_prefix;
+    if (threadIdx.x == 0) s_prefix = lookback_publish(lb, epoch, tile, (unsigned)total);
+    __syncthreads();
+    if (mine > 0) {
+        // append this thread's marked entries (its own keys, just written) in order
+        int pos = (int)s_prefix + excl;
+        for (int i = 0; i < kSchedPer; i++) {
+            const int p = p0 + i;
+            if (p >= N) break;
+            if (WEEKEND) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    const int b = keys[3 * (size_t)p + k];
+                    if (is_marked(mark, b)) {
+                        ckeys[pos] = (uint32_t)b;
+                        cvals[pos] = (uint32_t)p;
+                        pos++;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    const int b = keys[(size_t)k * N + p];
+                    if (is_marked(mark, b)) {
+                        ckeys[pos] = (uint32_t)b;
+                        cvals[pos] = (uint32_t)p;
+                        pos++;
+                    }
+                }
+            }
+        }
+    }
+    if (tile == (int)gridDim.x - 1 && threadIdx.x == 0) sc->marked_entries = (int)(s_prefix + total);
+    lookback_end(lb);
 }
 
 int day_buckets(const SimConst &c, bool weekend)
@@ -860,28 +960,39 @@ int day_buckets(const SimConst &c, bool weekend)
     return weekend ? 10 * (c.L - c.type_offset[9]) : 2 * (c.L - c.type_offset[8]);
 }
 
-cudaError_t launch_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s)
+// mark (or mark everything for complete tables), then the schedule kernel
+cudaError_t launch_schedule(const SimConst &c, const DevArrays &d, bool weekend, bool full_tables, cudaStream_t s)
 {
-    if (weekend) {
-        int blocks = std::min(div_up(c.N, 256), sm_count() * 32);
-        k_sched_weekend<<<std::max(1, blocks), 256, 0, s>>>(c, d.keys, d.bkt_count, d.sc);
-    } else {
-        int blocks = std::min(div_up(c.N / 2 + 1, 256), sm_count() * 32);
-        k_sched_weekday<<<std::max(1, blocks), 256, 0, s>>>(c, d.age, d.keys, d.bkt_count, d.sc);
+    const int B = day_buckets(c, weekend);
+    cudaError_t e = cudaMemsetAsync(d.mark, full_tables ? 0xFF : 0, ((size_t)B / 32 + 1) * 4, s);
+    if (e != cudaSuccess) return e;
+    if (!full_tables) {
+        k_mark_buckets<<<sm_count() * 4, 128, 0, s>>>(c, d.age, d.infected, weekend ? 1 : 0, d.mark, d.sc);
+        count_launch();
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
     }
+    const int blocks = std::max(1, div_up(c.N, kSchedTile));
+    LookBack lb = make_lb(d.tiles, d.tiles_cap, &d.sc->error);
+    if (weekend)
+        k_sched<true><<<blocks, kSchedThreads, 0, s>>>(c, d.age, d.mark, d.keys, d.bkt_count, d.rk1, d.rv1, d.sc, lb);
+    else
+        k_sched<false><<<blocks, kSchedThreads, 0, s>>>(c, d.age, d.mark, d.keys, d.bkt_count, d.rk1, d.rv1, d.sc, lb);
     count_launch();
     return cudaGetLastError();
 }
 
+// The day's radix sort starts from the marked entries the schedule appended to
+// (rk1, rv1), in person order; their count is on the device.
 static RadixArgs day_radix_args(const SimConst &c, const DevArrays &d, bool weekend)
 {
     RadixArgs r;
-    r.keys = (const uint32_t *)d.keys;
+    r.keys = d.rk1;
+    r.vals = d.rv1;
     r.E = (weekend ? 3 : 2) * c.N;
     r.buckets = day_buckets(c, weekend);
     r.N = c.N;
     r.person_mode = weekend ? 2 : 1;
-    r.mark = d.mark;
     r.count_dev = &d.sc->marked_entries;
     r.k0 = d.rk0; r.v0 = d.rv0; r.k1 = d.rk1; r.v1 = d.rv1;
     r.out = (uint32_t *)d.bkt_people;
@@ -893,40 +1004,13 @@ static RadixArgs day_radix_args(const SimConst &c, const DevArrays &d, bool week
     return r;
 }
 
-// Marks the errand buckets of today's infected: the only buckets the infection
-// kernels sample.  Every bucket of an infected person is marked (a superset of the
-// ones its contact profile uses).
-__global__ void k_mark_buckets(const int32_t *keys, const int32_t *infected, int N, int weekend, uint32_t *mark,
-                               const Scalars *sc)
+cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s)
 {
-    if (sc->done) return;
-    const int I = sc->infected;
-    const int per = weekend ? 3 : 2;
-    for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < I; pos += gridDim.x * blockDim.x) {
-        const int me = infected[pos];
-        for (int k = 0; k < per; k++) {
-            const int b = weekend ? keys[3 * (size_t)me + k] : keys[(size_t)k * N + me];
-            atomicOr(&mark[b >> 5], 1u << (b & 31));
-        }
-    }
-}
-
-cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weekend, bool full_tables, cudaStream_t s)
-{
-    RadixArgs r = day_radix_args(c, d, weekend);
-    const int P = radix_passes(r.buckets);
-    const size_t mark_bytes = ((size_t)r.buckets / 32 + 1) * 4;
-    cudaError_t e = cudaMemsetAsync(d.mark, full_tables ? 0xFF : 0, mark_bytes, s);
-    if (e != cudaSuccess) return e;
-    if (!full_tables) {
-        k_mark_buckets<<<sm_count() * 4, 256, 0, s>>>(d.keys, d.infected, c.N, weekend ? 1 : 0, d.mark, d.sc);
-        count_launch();
-        e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-    }
-    e = launch_scan_exclusive(d.bkt_count, d.bkt_offset, r.buckets, 1, d.tiles, (int *)(d.tiles + d.tiles_cap),
-                              &d.sc->error, &d.sc->done, P, d.digit_hist, s, d.mark, &d.sc->marked_entries,
-                              &d.sc->materialised_sum);
+    const int B = day_buckets(c, weekend);
+    const int P = radix_passes(B);
+    cudaError_t e = launch_scan_exclusive(d.bkt_count, d.bkt_offset, B, 1, d.tiles, (int *)(d.tiles + d.tiles_cap),
+                                          &d.sc->error, &d.sc->done, P, d.digit_hist, s, nullptr, nullptr,
+                                          &d.sc->materialised_sum);
     if (e != cudaSuccess) return e;
     k_digit_bases<<<1, 256, 0, s>>>(d.digit_hist, d.digit_base, P, &d.sc->done);
     count_launch();

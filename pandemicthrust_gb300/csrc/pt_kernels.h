@@ -96,6 +96,7 @@ cudaError_t launch_count_keys(const int32_t *keys, int n, int32_t *count, cudaSt
 struct RadixArgs {
     const uint32_t *keys;
     int E, buckets, N, person_mode;
+    const uint32_t *vals = nullptr;   // explicit input values (nullptr: implicit)
     const uint32_t *mark = nullptr;   // optional bucket filter of the first pass
     const int *count_dev = nullptr;   // entry count after the filter (device)
     uint32_t *k0, *v0, *k1, *v1, *out;
@@ -117,9 +118,9 @@ cudaError_t launch_seed_infected(const int32_t *seeds, int P, int S, uint32_t *s
 
 // ---- day
 cudaError_t launch_sweep(const SimConst &c, const DevArrays &d, int day, cudaStream_t s);
-cudaError_t launch_schedule(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
+cudaError_t launch_schedule(const SimConst &c, const DevArrays &d, bool weekend, bool full_tables, cudaStream_t s);
 int day_buckets(const SimConst &c, bool weekend);
-cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weekend, bool full_tables, cudaStream_t s);
+cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
 cudaError_t launch_bucket_sort(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
 cudaError_t launch_infect(const SimConst &c, const DevArrays &d, bool weekend, int day, cudaStream_t s);
 cudaError_t launch_apply(const DevArrays &d, int day, cudaStream_t s);

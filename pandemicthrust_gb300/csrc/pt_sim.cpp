@@ -346,9 +346,9 @@ static pt_status enqueue_day(pt_sim *s, int day)
     if (t) cudaEventRecord(stage_event(s, day, 0), st);
     CK(ptk::launch_sweep(c, d, day, st), "sweep");
     if (t) cudaEventRecord(stage_event(s, day, 1), st);
-    CK(ptk::launch_schedule(c, d, weekend, st), "schedule");
+    CK(ptk::launch_schedule(c, d, weekend, s->full_tables, st), "schedule");
     if (t) cudaEventRecord(stage_event(s, day, 2), st);
-    CK(ptk::launch_bucket_scan(c, d, weekend, s->full_tables, st), "bucket scan");
+    CK(ptk::launch_bucket_scan(c, d, weekend, st), "bucket scan");
     if (t) cudaEventRecord(stage_event(s, day, 3), st);
     CK(ptk::launch_bucket_sort(c, d, weekend, st), "bucket sort");
     if (t) cudaEventRecord(stage_event(s, day, 4), st);
