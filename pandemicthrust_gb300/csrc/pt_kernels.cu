@@ -425,8 +425,10 @@ __device__ __forceinline__ uint32_t pack_rank(unsigned d, unsigned rank, unsigne
 }
 
 // One stable radix pass over 8 bits of the keys.  FILTER (first pass only) drops
-// entries whose bucket is not set in `mark`; passes after a filtered first pass read
-// their entry count from *count_dev.
+// entries whose bucket is not set in `mark`; passes whose input count lives on the
+// device read it from *count_dev.  Persistent blocks take tiles from a ticket in
+// order until the entries run out, so a short input costs no idle blocks.  Look-back
+// words carry the launch epoch (see lb_word), so they need no reset between passes.
 template <int MODE>
 __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t *__restrict__ keys_in,
                                                                  const uint32_t *__restrict__ vals_in,
@@ -435,21 +437,25 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
                                                                  const int *count_dev, const uint32_t *mark,
                                                                  int shift, int nbits, int N, int person_mode,
                                                                  const int *__restrict__ digit_base,
-                                                                 uint32_t *status, int *ctl, int *error,
+                                                                 unsigned long long *status, int *ctl, int *error,
                                                                  const int *skip)
 {
     if (skip && *(volatile const int *)skip) return;
     __shared__ int s_tile;
+    __shared__ unsigned s_epoch;
     __shared__ int s_hist[kRadixWarps][256];
     __shared__ int s_base[256];
-    if (threadIdx.x == 0) s_tile = atomicAdd(&ctl[0], 1);
-    for (int i = threadIdx.x; i < kRadixWarps * 256; i += kRadixThreads) (&s_hist[0][0])[i] = 0;
-    __syncthreads();
-    const int tile = s_tile;
     const int E = count_dev ? *(volatile const int *)count_dev : E_arg;
-    if (tile * kRadixTile < E) {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        const unsigned lt = (1u << lane) - 1u;
+    if (threadIdx.x == 0) s_epoch = (unsigned)(*(volatile int *)&ctl[2]) & 0x3FFFFFFFu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(&ctl[0], 1);
+        for (int i = threadIdx.x; i < kRadixWarps * 256; i += kRadixThreads) (&s_hist[0][0])[i] = 0;
+        __syncthreads();
+        const int tile = s_tile;
+        const unsigned epoch = s_epoch;
+        if ((long long)tile * kRadixTile >= E) break;
         const int base = tile * kRadixTile + warp * kRadixWarpItems + lane;
         const bool full = (tile + 1) * kRadixTile <= E;
         uint32_t key[kRadixItems], val[kRadixItems], info[kRadixItems];
@@ -489,18 +495,18 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
                 s_hist[w][d] = run;
                 run += c;
             }
-            volatile uint32_t *st = status;
+            volatile unsigned long long *st = status;
             int excl = 0;
             if (tile == 0) {
-                st[d] = (2u << 30) | (uint32_t)run;
+                st[d] = lb_word(epoch, 2, (unsigned)run);
             } else {
-                st[(size_t)tile * 256 + d] = (1u << 30) | (uint32_t)run;
+                st[(size_t)tile * 256 + d] = lb_word(epoch, 1, (unsigned)run);
                 int t = tile - 1;
                 long long spins = 0;
                 while (t >= 0) {
-                    const uint32_t w = st[(size_t)t * 256 + d];
-                    const uint32_t flag = w >> 30;
-                    if (flag == 0) {
+                    const unsigned long long w = st[(size_t)t * 256 + d];
+                    const unsigned flag = (unsigned)(w >> 32) & 3u;
+                    if ((unsigned)(w >> 34) != epoch || flag == 0) {
                         if (++spins > kSpinLimit) {
                             atomicExch(error, 2);
                             break;
@@ -508,11 +514,11 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
                         __nanosleep(32);
                         continue;
                     }
-                    excl += (int)(w & 0x3FFFFFFFu);
+                    excl += (int)(unsigned)w;
                     if (flag == 2) break;
                     t--;
                 }
-                st[(size_t)tile * 256 + d] = (2u << 30) | (uint32_t)(excl + run);
+                st[(size_t)tile * 256 + d] = lb_word(epoch, 2, (unsigned)(excl + run));
             }
             s_base[d] = digit_base[d] + excl;
         }
@@ -533,6 +539,7 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
             }
             __syncwarp();
         }
+        __syncthreads();
     }
     if (threadIdx.x == 0) {
         __threadfence();
@@ -540,6 +547,7 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
         if (fin == (int)gridDim.x - 1) {
             ctl[0] = 0;
             ctl[1] = 0;
+            atomicAdd(&ctl[2], 1);
             __threadfence();
         }
     }
@@ -559,12 +567,12 @@ cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
     const int P = radix_passes(r.buckets);
     const int bits = key_bits(r.buckets);
     const int tiles = std::max(1, div_up(r.E, kRadixTile));
+    const int grid = std::max(1, std::min(tiles, 3 * sm_count()));  // persistent blocks
     const uint32_t *kin = r.keys;
     const uint32_t *vin = r.vals;   // nullptr: implicit values (entry index -> person)
     const bool implicit = r.vals == nullptr;
     for (int p = 0; p < P; p++) {
-        cudaError_t e = cudaMemsetAsync(r.status, 0, (size_t)tiles * 256 * sizeof(uint32_t), s);
-        if (e != cudaSuccess) return e;
+        cudaError_t e;
         uint32_t *kout = (p & 1) ? r.k1 : r.k0;
         uint32_t *vout = (p == P - 1) ? r.out : ((p & 1) ? r.v1 : r.v0);
         const int *db = r.digit_base + 256 * p;
@@ -576,13 +584,13 @@ cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
         const uint32_t *mk = (p == 0) ? r.mark : nullptr;
 #define PT_RADIX_ARGS kin, vin, kout, vout, r.E, cnt, mk, shift, nbits, r.N, r.person_mode, db, r.status, r.ctl, r.error, r.skip
         if (P == 1 && implicit)
-            k_radix_pass<kRadixOnly><<<tiles, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+            k_radix_pass<kRadixOnly><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
         else if (p == 0 && implicit)
-            k_radix_pass<kRadixFirst><<<tiles, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+            k_radix_pass<kRadixFirst><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
         else if (p == P - 1)
-            k_radix_pass<kRadixLast><<<tiles, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+            k_radix_pass<kRadixLast><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
         else
-            k_radix_pass<kRadixMiddle><<<tiles, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+            k_radix_pass<kRadixMiddle><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
 #undef PT_RADIX_ARGS
         count_launch();
         e = cudaGetLastError();
@@ -853,11 +861,26 @@ __global__ void k_mark_buckets(SimConst c, const uint8_t *age, const int32_t *in
     }
 }
 
-// Schedule kernel, one tile of 4096 persons per block (16 contiguous persons per
-// thread).  It writes every person's keys, counts the entries of marked buckets and
-// appends those entries as (key, person) in ascending person order (block scan +
-// decoupled look-back), the order the radix sort needs for stability.
-constexpr int kSchedThreads = 256, kSchedPer = 16, kSchedTile = kSchedThreads * kSchedPer;
+// Schedule kernel, one tile of 4096 persons per block.  Warps own 512 consecutive
+// persons and walk them in rounds (weekday: 64 persons a round, a pair per lane, one
+// Threefry block per pair; weekend: 32 persons a round, one per lane), so key writes
+// are coalesced.  The kernel writes every person's keys, counts the entries of
+// marked buckets and appends those entries as (key, person) in ascending person
+// order (warp scans + block scan + decoupled look-back): the order the radix sort
+// needs for stability.  Per-round marked counts of a lane are packed in one register
+// between the two phases.
+constexpr int kSchedThreads = 256, kSchedTile = 4096, kSchedWarpPersons = 512;
+
+__device__ __forceinline__ int warp_inclusive_scan(int v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    return v;
+}
 
 template <bool WEEKEND>
 __global__ void __launch_bounds__(kSchedThreads) k_sched(SimConst c, const uint8_t *age, const uint32_t *mark,
@@ -871,64 +894,97 @@ __global__ void __launch_bounds__(kSchedThreads) k_sched(SimConst c, const uint8
     const TfKey key = make_key(c);
     const unsigned long long E0 = sc->errand_offset;
     const int N = c.N;
-    const int p0 = tile * kSchedTile + threadIdx.x * kSchedPer;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wbase = tile * kSchedTile + warp * kSchedWarpPersons;
+    constexpr int kRounds = WEEKEND ? 16 : 8;
+    constexpr int kBits = WEEKEND ? 2 : 3;  // marked entries per lane and round: <= 3 / <= 4
+    uint32_t cpack = 0;
     int mine = 0;
     if (WEEKEND) {
         // kernel_assignWeekendErrands (PandemicSim.cu:2082-2094): counters E0 + 2p, E0 + 2p + 1
         const int lo = c.type_offset[9], R = c.L - lo;
-        for (int i = 0; i < kSchedPer; i++) {
-            const int p = p0 + i;
-            if (p >= N) break;
-            int d[3];
-            weekend_errands(c, key, E0 + 2ull * (unsigned long long)p, lo, R, d);
+#pragma unroll 1
+        for (int j = 0; j < kRounds; j++) {
+            const int p = wbase + 32 * j + lane;
+            int cnt = 0;
+            if (p < N) {
+                int d[3];
+                weekend_errands(c, key, E0 + 2ull * (unsigned long long)p, lo, R, d);
 #pragma unroll
-            for (int k = 0; k < 3; k++) {
-                keys[3 * (size_t)p + k] = d[k];
-                if (is_marked(mark, d[k])) {
-                    atomicAdd(&count[d[k]], 1);
-                    mine++;
+                for (int k = 0; k < 3; k++) {
+                    keys[3 * (size_t)p + k] = d[k];
+                    if (is_marked(mark, d[k])) {
+                        atomicAdd(&count[d[k]], 1);
+                        cnt++;
+                    }
                 }
             }
+            cpack |= (uint32_t)cnt << (kBits * j);
+            mine += cnt;
         }
     } else {
         const int lo = c.type_offset[8], R = c.L - lo;
-        for (int i = 0; i < kSchedPer; i += 2) {
-            const int p = p0 + i;  // even: counter E0 + p/2 covers persons p, p+1
-            if (p >= N) break;
-            uint32_t w[4];
-            tf2x64(key, E0 + (uint64_t)(p / 2), w);
+#pragma unroll 1
+        for (int j = 0; j < kRounds; j++) {
+            const int p = wbase + 64 * j + 2 * lane;  // even: counter E0 + p/2 covers p, p+1
+            int cnt = 0;
+            if (p < N) {
+                uint32_t w[4];
+                tf2x64(key, E0 + (uint64_t)(p / 2), w);
 #pragma unroll
-            for (int k = 0; k < 2; k++) {
-                const int q = p + k;
-                if (q < N) {
-                    int k1, k2;
-                    weekday_pair_keys(c, w, k, age[q] == 5, lo, R, k1, k2);
-                    keys[q] = k1;
-                    keys[(size_t)N + q] = k2;
-                    if (is_marked(mark, k1)) {
-                        atomicAdd(&count[k1], 1);
-                        mine++;
-                    }
-                    if (is_marked(mark, k2)) {
-                        atomicAdd(&count[k2], 1);
-                        mine++;
+                for (int k = 0; k < 2; k++) {
+                    const int q = p + k;
+                    if (q < N) {
+                        int k1, k2;
+                        weekday_pair_keys(c, w, k, age[q] == 5, lo, R, k1, k2);
+                        keys[q] = k1;
+                        keys[(size_t)N + q] = k2;
+                        if (is_marked(mark, k1)) {
+                            atomicAdd(&count[k1], 1);
+                            cnt++;
+                        }
+                        if (is_marked(mark, k2)) {
+                            atomicAdd(&count[k2], 1);
+                            cnt++;
+                        }
                     }
                 }
             }
+            cpack |= (uint32_t)cnt << (kBits * j);
+            mine += cnt;
         }
     }
-    int total;
-    const int excl = block_exclusive_scan<kSchedThreads, int>(mine, total);
-    __shared__ unsigned s_prefix;
-    if (threadIdx.x == 0) s_prefix = lookback_publish(lb, epoch, tile, (unsigned)total);
+    // tile position: warp totals, block scan over warps, look-back
+    __shared__ int s_wtot[kSchedThreads / 32];
+    __shared__ int s_wbase[kSchedThreads / 32];
+    int wt = mine;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wt += __shfl_xor_sync(0xffffffffu, wt, o);
+    if (lane == 0) s_wtot[warp] = wt;
     __syncthreads();
-    if (mine > 0) {
-        // append this thread's marked entries (its own keys, just written) in order
-        int pos = (int)s_prefix + excl;
-        for (int i = 0; i < kSchedPer; i++) {
-            const int p = p0 + i;
-            if (p >= N) break;
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int w = 0; w < kSchedThreads / 32; w++) {
+            s_wbase[w] = run;
+            run += s_wtot[w];
+        }
+        const unsigned prefix = lookback_publish(lb, epoch, tile, (unsigned)run);
+        for (int w = 0; w < kSchedThreads / 32; w++) s_wbase[w] += (int)prefix;
+        if (tile == (int)gridDim.x - 1) sc->marked_entries = (int)prefix + run;
+    }
+    __syncthreads();
+    // append the marked entries, rounds in order, lanes in order within a round
+    int run = s_wbase[warp];
+    const uint32_t cmask = (1u << kBits) - 1u;
+#pragma unroll 1
+    for (int j = 0; j < kRounds; j++) {
+        const int cnt = (int)((cpack >> (kBits * j)) & cmask);
+        if (__ballot_sync(0xffffffffu, cnt > 0) == 0) continue;
+        const int incl = warp_inclusive_scan(cnt);
+        int pos = run + incl - cnt;
+        if (cnt > 0) {
             if (WEEKEND) {
+                const int p = wbase + 32 * j + lane;
 #pragma unroll
                 for (int k = 0; k < 3; k++) {
                     const int b = keys[3 * (size_t)p + k];
@@ -939,19 +995,26 @@ __global__ void __launch_bounds__(kSchedThreads) k_sched(SimConst c, const uint8
                     }
                 }
             } else {
+                const int p = wbase + 64 * j + 2 * lane;
 #pragma unroll
                 for (int k = 0; k < 2; k++) {
-                    const int b = keys[(size_t)k * N + p];
-                    if (is_marked(mark, b)) {
-                        ckeys[pos] = (uint32_t)b;
-                        cvals[pos] = (uint32_t)p;
-                        pos++;
+                    const int q = p + k;
+                    if (q < N) {
+#pragma unroll
+                        for (int h = 0; h < 2; h++) {
+                            const int b = keys[(size_t)h * N + q];
+                            if (is_marked(mark, b)) {
+                                ckeys[pos] = (uint32_t)b;
+                                cvals[pos] = (uint32_t)q;
+                                pos++;
+                            }
+                        }
                     }
                 }
             }
         }
+        run += __shfl_sync(0xffffffffu, incl, 31);
     }
-    if (tile == (int)gridDim.x - 1 && threadIdx.x == 0) sc->marked_entries = (int)(s_prefix + total);
     lookback_end(lb);
 }
 

@@ -62,7 +62,7 @@ struct DevArrays {
     int32_t *bkt_count;       // buckets histogram, zero between uses
     int32_t *bkt_people;      // 3N person ids bucket by bucket, ascending in each
     uint32_t *rk0, *rv0, *rk1, *rv1;  // 3N each: radix ping-pong keys/values
-    uint32_t *radix_status;   // ceil(3N/4096) x 256 look-back words per pass
+    unsigned long long *radix_status;  // ceil(3N/4096) x 256 epoch-tagged look-back words
     int *radix_ctl;           // ticket, finished
     int *digit_hist;          // 4 x 256
     int *digit_base;          // 4 x 256
@@ -101,8 +101,8 @@ struct RadixArgs {
     const int *count_dev = nullptr;   // entry count after the filter (device)
     uint32_t *k0, *v0, *k1, *v1, *out;
     const int *digit_base;
-    uint32_t *status;
-    int *ctl;
+    unsigned long long *status;   // look-back words, ceil(E/4096) x 256, epoch-tagged
+    int *ctl;                     // ticket, finished, epoch
     int *error;
     const int *skip;
 };

@@ -243,7 +243,7 @@ pt_status pt_setup(pt_sim *s)
     bytes += round256(3 * n * 4) * 6;         // keys, bkt_people, radix k0/v0/k1/v1
     bytes += round256((B + 1) * 4);           // bkt_offset
     bytes += round256(B * 4);                 // bkt_count
-    bytes += round256(radix_tiles * 256 * 4); // radix look-back words
+    bytes += round256(radix_tiles * 256 * 8); // radix look-back words
     bytes += round256(8 * 4) + 2 * round256(4 * 256 * 4);  // radix ctl, digit hist/base
     bytes += round256((B / 32 + 1) * 4);      // bucket mark bitmap
     bytes += round256(n * 4);                 // infected
@@ -269,7 +269,7 @@ pt_status pt_setup(pt_sim *s)
     d.rv1 = a.take<uint32_t>(3 * n);
     d.bkt_offset = a.take<int32_t>(B + 1);
     d.bkt_count = a.take<int32_t>(B);
-    d.radix_status = a.take<uint32_t>(radix_tiles * 256);
+    d.radix_status = a.take<unsigned long long>(radix_tiles * 256);
     d.radix_ctl = a.take<int>(8);
     d.digit_hist = a.take<int>(4 * 256);
     d.digit_base = a.take<int>(4 * 256);
@@ -280,6 +280,7 @@ pt_status pt_setup(pt_sim *s)
     s->d_seeds = a.take<int32_t>((size_t)(P + S + 1));
     CK(cudaMemsetAsync(d.bkt_count, 0, B * 4, s->stream), "memset counts");
     CK(cudaMemsetAsync(d.radix_ctl, 0, 8 * 4, s->stream), "memset radix ctl");
+    CK(cudaMemsetAsync(d.radix_status, 0, radix_tiles * 256 * 8, s->stream), "memset radix words");
     CK(cudaMemsetAsync(d.digit_hist, 0, 4 * 256 * 4, s->stream), "memset digit hist");
 
     // households -> persons, then workplaces and schools (setup_assignWorkplaces)

@@ -38,7 +38,7 @@ constexpr size_t kOffV0 = kOffK0 + align256((size_t)kMaxEntries * 4);
 constexpr size_t kOffK1 = kOffV0 + align256((size_t)kMaxEntries * 4);
 constexpr size_t kOffV1 = kOffK1 + align256((size_t)kMaxEntries * 4);
 constexpr size_t kOffStatus = kOffV1 + align256((size_t)kMaxEntries * 4);         // radix look-back words
-constexpr size_t kOffScanTiles = kOffStatus + align256((size_t)kRadixTiles * 256 * 4);  // scan look-back words + control
+constexpr size_t kOffScanTiles = kOffStatus + align256((size_t)kRadixTiles * 256 * 8);  // scan look-back words + control
 constexpr size_t kOffRadixCtl = kOffScanTiles + align256((size_t)(kScanTiles + 4) * 8);
 constexpr size_t kOffDigitHist = kOffRadixCtl + 256;
 constexpr size_t kOffDigitBase = kOffDigitHist + align256(4 * 256 * 4);
@@ -96,6 +96,7 @@ extern "C" pt_status pt_bucket_table_static(const int32_t *keys, int n, int buck
     if (cudaMemsetAsync(counts, 0, (size_t)buckets * 4, s) != cudaSuccess) return PT_ERR_CUDA;
     if (cudaMemsetAsync(scan_tiles, 0, (size_t)(kScanTiles + 4) * 8, s) != cudaSuccess) return PT_ERR_CUDA;
     if (cudaMemsetAsync(base + kOffRadixCtl, 0, 256, s) != cudaSuccess) return PT_ERR_CUDA;
+    if (cudaMemsetAsync(base + kOffStatus, 0, (size_t)kRadixTiles * 256 * 8, s) != cudaSuccess) return PT_ERR_CUDA;
     if (cudaMemsetAsync(base + kOffDigitHist, 0, 4 * 256 * 4, s) != cudaSuccess) return PT_ERR_CUDA;
     if (cudaMemsetAsync(error, 0, sizeof(int), s) != cudaSuccess) return PT_ERR_CUDA;
     int herr = 0;
@@ -120,7 +121,7 @@ extern "C" pt_status pt_bucket_table_static(const int32_t *keys, int n, int buck
     r.v1 = (uint32_t *)(base + kOffV1);
     r.out = (uint32_t *)table;
     r.digit_base = (const int *)(base + kOffDigitBase);
-    r.status = (uint32_t *)(base + kOffStatus);
+    r.status = (unsigned long long *)(base + kOffStatus);
     r.ctl = (int *)(base + kOffRadixCtl);
     r.error = error;
     r.skip = nullptr;
