@@ -3,17 +3,20 @@
 The reference's simulation kernels are plain C++ inside ``__global__``/``__device__``
 functions, so the hot-path slices of PandemicThrust/PandemicThrust/PandemicSim.cu
 compile for the host once the CUDA qualifiers are defined away.  This script copies
-the cited line ranges, verbatim and in order, into ``oracle/_ref/ref_slices.inc``
-(a build product, git-ignored: reference source never enters the repository) and
-compiles them with ``oracle/ref_harness.cpp``, which restates the host flow of
-``class PandemicSim`` around them, plus the reference's own ``host_functions.cpp``.
+the cited line ranges, verbatim and in order, into a temporary include file (deleted
+after the build: reference source never enters the repository) and compiles them
+with ``oracle/ref_harness.cpp``, which restates the host flow of ``class
+PandemicSim`` around them, plus the reference's own ``host_functions.cpp``.  Only
+the shared library ``oracle/_ref/libptref.so`` is kept.
 
 Run here, where the reference tree exists:  python oracle/build_ref.py
 The GPU test box has no reference tree; the tests that need this library skip there.
 """
 import os
+import shutil
 import subprocess
 import sys
+import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
@@ -68,20 +71,27 @@ def build(verbose=False):
             print("reference tree not present; oracle/_ref not built")
         return None
     os.makedirs(OUT, exist_ok=True)
-    inc = os.path.join(OUT, "ref_slices.inc")
-    write_slices(inc)
-    so = os.path.join(OUT, "libptref.so")
-    cmd = [
-        "g++", "-std=c++20", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
-        "-w", "-Wno-narrowing",
-        "-I", OUT, "-I", R123_DIR, "-I", SRC_DIR, "-I", HERE,
-        os.path.join(HERE, "ref_harness.cpp"),
-        os.path.join(SRC_DIR, "host_functions.cpp"),
-        "-o", so,
-    ]
-    if verbose:
-        print(" ".join(cmd))
-    subprocess.check_call(cmd)
+    stale = os.path.join(OUT, "ref_slices.inc")
+    if os.path.exists(stale):
+        os.remove(stale)
+    tmp = tempfile.mkdtemp(prefix="ptref_")
+    try:
+        inc = os.path.join(tmp, "ref_slices.inc")
+        write_slices(inc)
+        so = os.path.join(OUT, "libptref.so")
+        cmd = [
+            "g++", "-std=c++20", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
+            "-w", "-Wno-narrowing",
+            "-I", tmp, "-I", R123_DIR, "-I", SRC_DIR, "-I", HERE,
+            os.path.join(HERE, "ref_harness.cpp"),
+            os.path.join(SRC_DIR, "host_functions.cpp"),
+            "-o", so,
+        ]
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.check_call(cmd)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
     return so
 
 

@@ -446,16 +446,21 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
     __shared__ int s_hist[kRadixWarps][256];
     __shared__ int s_base[256];
     const int E = count_dev ? *(volatile const int *)count_dev : E_arg;
+    // only as many blocks as there are tiles take part (ticket, finish count)
+    const int tiles = (E + kRadixTile - 1) / kRadixTile;
+    const int active = tiles < (int)gridDim.x ? tiles : (int)gridDim.x;
+    if ((int)blockIdx.x >= active) return;
     if (threadIdx.x == 0) s_epoch = (unsigned)(*(volatile int *)&ctl[2]) & 0x3FFFFFFFu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(&ctl[0], 1);
-        for (int i = threadIdx.x; i < kRadixWarps * 256; i += kRadixThreads) (&s_hist[0][0])[i] = 0;
         __syncthreads();
         const int tile = s_tile;
         const unsigned epoch = s_epoch;
-        if ((long long)tile * kRadixTile >= E) break;
+        if (tile >= tiles) break;
+        for (int i = threadIdx.x; i < kRadixWarps * 256; i += kRadixThreads) (&s_hist[0][0])[i] = 0;
+        __syncthreads();
         const int base = tile * kRadixTile + warp * kRadixWarpItems + lane;
         const bool full = (tile + 1) * kRadixTile <= E;
         uint32_t key[kRadixItems], val[kRadixItems], info[kRadixItems];
@@ -544,7 +549,7 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
     if (threadIdx.x == 0) {
         __threadfence();
         const int fin = atomicAdd(&ctl[1], 1);
-        if (fin == (int)gridDim.x - 1) {
+        if (fin == active - 1) {
             ctl[0] = 0;
             ctl[1] = 0;
             atomicAdd(&ctl[2], 1);
@@ -830,33 +835,46 @@ __device__ __forceinline__ void weekday_pair_keys(const SimConst &c, const uint3
 
 __device__ __forceinline__ bool is_marked(const uint32_t *mark, int b) { return (mark[b >> 5] >> (b & 31)) & 1u; }
 
-// Marks the errand buckets of today's infected: the only buckets the contact draws
-// read.  Their destinations are regenerated from the schedule counter, as the
-// reference's device_recalc_* functions do (PandemicSim.cu:3667-3705, :3742-3746).
-// Every errand of an infected person is marked, a superset of the ones its contact
-// profile uses.
+// Marks the errand buckets today's contact draws will read: the only buckets that
+// must be materialised.  Destinations are regenerated from the schedule counter, as
+// the reference's device_recalc_* functions do (PandemicSim.cu:3667-3705,
+// :3742-3746), and only the hours / errands the person's contact profile uses are
+// marked: weekday hours whose profile wants contacts (the adult profile comes from
+// the same Threefry block, :3697-3702; children use the afterschool profile), and on
+// weekends the two errand slots picked by word 3 of the infection counter's block
+// (:1892, :1909, :1929).
 __global__ void k_mark_buckets(SimConst c, const uint8_t *age, const int32_t *infected, int weekend, uint32_t *mark,
                                const Scalars *sc)
 {
     if (sc->done) return;
     const TfKey key = make_key(c);
     const int I = sc->infected;
-    const unsigned long long E0 = sc->errand_offset;
+    const unsigned long long E0 = sc->errand_offset, R0 = sc->infect_offset;
     for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < I; pos += gridDim.x * blockDim.x) {
         const int me = infected[pos];
         if (weekend) {
             const int lo = c.type_offset[9], R = c.L - lo;
             int d[3];
             weekend_errands(c, key, E0 + 2ull * (unsigned long long)me, lo, R, d);
-            for (int k = 0; k < 3; k++) atomicOr(&mark[d[k] >> 5], 1u << (d[k] & 31));
+            uint32_t w[4];
+            tf2x64(key, R0 + 6ull * (unsigned long long)pos, w);
+            const int prof = (int)(w[3] % 6u);
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const int b = d[c_weekend_assign[prof][k]];
+                atomicOr(&mark[b >> 5], 1u << (b & 31));
+            }
         } else {
             const int lo = c.type_offset[8], R = c.L - lo;
             uint32_t w[4];
             tf2x64(key, E0 + (uint64_t)(me / 2), w);
+            const bool adult = age[me] == 5;
+            const int slot = 2 * (me & 1);
             int k1, k2;
-            weekday_pair_keys(c, w, me & 1, age[me] == 5, lo, R, k1, k2);
-            atomicOr(&mark[k1 >> 5], 1u << (k1 & 31));
-            atomicOr(&mark[k2 >> 5], 1u << (k2 & 31));
+            weekday_pair_keys(c, w, me & 1, adult, lo, R, k1, k2);
+            const int prof = adult ? (int)((w[slot] ^ w[slot + 1]) % 3u) : 3;
+            if (c_weekday_assign[prof][0] > 0) atomicOr(&mark[k1 >> 5], 1u << (k1 & 31));
+            if (c_weekday_assign[prof][1] > 0) atomicOr(&mark[k2 >> 5], 1u << (k2 & 31));
         }
     }
 }
