@@ -140,6 +140,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def reduce_replicas(ms, person_days, device):
+    """Whole-job figures over replica ranks: total person-days and the slowest rank's
+    time (max over ranks).  One independent simulation per rank, no data exchange."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    pd = torch.tensor([float(person_days)], device=device, dtype=torch.float64)
+    dist.all_reduce(pd)
+    return float(t.item()), float(pd.item())
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -268,12 +280,7 @@ def main():
     launches = pt.launch_count() - launches0
     ms = start.elapsed_time(end)
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-        pd = torch.tensor([float(N) * days_total], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(pd)
-        person_days = float(pd.item())
+        ms, person_days = reduce_replicas(ms, float(N) * days_total, "cuda")
     else:
         person_days = float(N) * days_total
     value = person_days / (ms / 1000.0)
