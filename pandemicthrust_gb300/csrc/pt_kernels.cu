@@ -444,7 +444,10 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
     __shared__ int s_tile;
     __shared__ unsigned s_epoch;
     __shared__ int s_hist[kRadixWarps][256];
-    __shared__ int s_base[256];
+    __shared__ int s_base[256];   // global position of the tile's first entry of each digit
+    __shared__ int s_toff[256];   // tile-local position of each digit's first entry
+    __shared__ uint32_t s_key[kRadixTile];
+    __shared__ uint32_t s_val[kRadixTile];
     const int E = count_dev ? *(volatile const int *)count_dev : E_arg;
     // only as many blocks as there are tiles take part (ticket, finish count)
     const int tiles = (E + kRadixTile - 1) / kRadixTile;
@@ -526,9 +529,14 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
                 st[(size_t)tile * 256 + d] = lb_word(epoch, 2, (unsigned)(excl + run));
             }
             s_base[d] = digit_base[d] + excl;
+            // tile-local start of digit d (entries of the tile ordered by digit)
+            int tile_total;
+            const int toff = block_exclusive_scan<kRadixThreads, int>(run, tile_total);
+            s_toff[d] = toff;
+            if (d == 0) s_tile = tile_total;  // reuse: valid entries of this tile
         }
         __syncthreads();
-        // phase B: write each entry at its global position
+        // phase B: place each entry in shared memory in digit order (stable) ...
 #pragma unroll
         for (int j = 0; j < kRadixItems; j++) {
             const uint32_t r = info[j];
@@ -537,12 +545,22 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
             const int wbase = ok ? s_hist[warp][d] : 0;
             __syncwarp();
             if (ok) {
-                const int pos = s_base[d] + wbase + (int)rank;
-                if (MODE == kRadixFirst || MODE == kRadixMiddle) keys_out[pos] = key[j];
-                vals_out[pos] = val[j];
+                const int lpos = s_toff[d] + wbase + (int)rank;
+                s_key[lpos] = key[j];
+                s_val[lpos] = val[j];
                 if (rank == 0) s_hist[warp][d] = wbase + (int)cnt;
             }
             __syncwarp();
+        }
+        __syncthreads();
+        // ... then write each digit's run with consecutive threads (coalesced)
+        const int valid = s_tile;
+        for (int i = threadIdx.x; i < valid; i += kRadixThreads) {
+            const uint32_t k = s_key[i];
+            const unsigned d = (k >> shift) & 255u;
+            const int pos = s_base[d] + (i - s_toff[d]);
+            if (MODE == kRadixFirst || MODE == kRadixMiddle) keys_out[pos] = k;
+            vals_out[pos] = s_val[i];
         }
         __syncthreads();
     }
@@ -678,6 +696,8 @@ cudaError_t launch_seed_infected(const int32_t *seeds, int P, int S, uint32_t *s
 // which is ascending person order within the tile.
 constexpr int kSweepThreads = 256, kSweepRounds = 4, kSweepTile = kSweepThreads * 4 * kSweepRounds;
 
+constexpr uint32_t kNeverInfected = 0x01u | (0x01u << 8) | (0xFFu << 16) | (0xFFu << 24);
+
 __device__ __forceinline__ uint32_t recover_word(uint32_t st, int d2r, bool &changed)
 {
     uint32_t sp = st & 0xFFu, ss = (st >> 8) & 0xFFu, dp = (st >> 16) & 0xFFu, ds = st >> 24;
@@ -700,6 +720,7 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(SimConst c, uint32_t *s
     const long long tile_base = (long long)tile * kSweepTile;
     // packed per-thread status bins: 16-bit fields, bins 0-3 / 4-7 per strain
     unsigned long long bp_lo = 0, bp_hi = 0, bs_lo = 0, bs_hi = 0;
+    int nss = 0;         // persons in the never-infected state (S, S, day 255, day 255)
     uint32_t flags = 0;  // bit (4*round + item)
     unsigned long long packed_counts = 0;
 #pragma unroll
@@ -718,6 +739,12 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(SimConst c, uint32_t *s
         int cnt = 0;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
+            // never infected by either strain: nothing to recover, bin S twice
+            if (st[j] == kNeverInfected && p0 + j < N) {
+                out[j] = st[j];
+                nss++;
+                continue;
+            }
             bool ch;
             out[j] = recover_word(st[j], d2r, ch);
             if (p0 + j < N) {
@@ -743,6 +770,8 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(SimConst c, uint32_t *s
         packed_counts |= (unsigned long long)cnt << (16 * r);
     }
     // status bins: warp reduction then one atomic per bin per warp
+    bp_lo += (unsigned long long)nss << 16;  // bin 1 (S) of each strain
+    bs_lo += (unsigned long long)nss << 16;
     __shared__ int s_bins[16];
     if (threadIdx.x < 16) s_bins[threadIdx.x] = 0;
     __syncthreads();
