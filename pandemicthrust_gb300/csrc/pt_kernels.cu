@@ -59,36 +59,47 @@ __device__ __forceinline__ unsigned long long lb_word(unsigned epoch, unsigned f
     return ((unsigned long long)epoch << 34) | ((unsigned long long)flag << 32) | value;
 }
 
-// Called by one thread.  Publishes the tile aggregate, walks back to the nearest
-// inclusive prefix, publishes the tile's inclusive prefix and returns the exclusive one.
-__device__ unsigned lookback_publish(const LookBack &lb, unsigned epoch, int tile, unsigned aggregate)
+// Called by all 32 lanes of one warp.  Publishes the tile aggregate, then walks back
+// 32 predecessors per step (one word per lane) to the nearest inclusive prefix,
+// publishes the tile's inclusive prefix and returns the exclusive one on every lane.
+__device__ unsigned lookback_publish_warp(const LookBack &lb, unsigned epoch, int tile, unsigned aggregate)
 {
     volatile unsigned long long *t = lb.tiles;
+    const int lane = threadIdx.x & 31;
     if (tile == 0) {
-        t[0] = lb_word(epoch, 2, aggregate);
+        if (lane == 0) t[0] = lb_word(epoch, 2, aggregate);
         return 0;
     }
-    t[tile] = lb_word(epoch, 1, aggregate);
+    if (lane == 0) t[tile] = lb_word(epoch, 1, aggregate);
     unsigned excl = 0;
-    int j = tile - 1;
+    int top = tile - 1;  // the window covers tiles top, top-1, ..., top-31
     long long spins = 0;
-    while (j >= 0) {
-        unsigned long long w = t[j];
-        unsigned ep = (unsigned)(w >> 34);
-        unsigned flag = (unsigned)(w >> 32) & 3u;
-        if (ep != (epoch & 0x3FFFFFFFu) || flag == 0) {
-            if (++spins > kSpinLimit) {
-                atomicExch(lb.error, 1);
-                break;
-            }
-            __nanosleep(64);
+    while (true) {
+        const int j = top - lane;
+        unsigned long long w = j >= 0 ? t[j] : lb_word(epoch, 2, 0);  // before tile 0: prefix 0
+        const bool ready = (unsigned)(w >> 34) == (epoch & 0x3FFFFFFFu) && ((unsigned)(w >> 32) & 3u) != 0;
+        const bool prefix = ready && ((unsigned)(w >> 32) & 3u) == 2;
+        const unsigned rmask = __ballot_sync(0xffffffffu, ready);
+        const unsigned pmask = __ballot_sync(0xffffffffu, prefix);
+        // lanes up to (and including) the closest prefix must all be ready
+        const int stop = pmask ? __ffs(pmask) - 1 : 31;
+        const unsigned need = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
+        if ((rmask & need) == need) {
+            unsigned v = (lane <= stop) ? (unsigned)w : 0u;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            excl += v;
+            if (pmask) break;
+            top -= 32;
             continue;
         }
-        excl += (unsigned)w;
-        if (flag == 2) break;
-        j--;
+        if (++spins > kSpinLimit) {
+            if (lane == 0) atomicExch(lb.error, 1);
+            break;
+        }
+        __nanosleep(64);
     }
-    t[tile] = lb_word(epoch, 2, excl + aggregate);
+    if (lane == 0) t[tile] = lb_word(epoch, 2, excl + aggregate);
     return excl;
 }
 
@@ -242,7 +253,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *in, int32_
     int total;
     int excl = block_exclusive_scan<kScanThreads, int>(sum, total);
     __shared__ unsigned s_prefix;
-    if (threadIdx.x == 0) s_prefix = lookback_publish(lb, epoch, tile, (unsigned)total);
+    if (threadIdx.x < 32) {
+        const unsigned e = lookback_publish_warp(lb, epoch, tile, (unsigned)total);
+        if (threadIdx.x == 0) s_prefix = e;
+    }
     __syncthreads();
     int run = (int)s_prefix + excl;
 #pragma unroll
@@ -804,7 +818,10 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(SimConst c, uint32_t *s
         tile_total += (unsigned)((round_tot >> (16 * r)) & 0xFFFF);
     }
     __shared__ unsigned s_prefix;
-    if (threadIdx.x == 0) s_prefix = lookback_publish(lb, epoch, tile, tile_total);
+    if (threadIdx.x < 32) {
+        const unsigned e = lookback_publish_warp(lb, epoch, tile, tile_total);
+        if (threadIdx.x == 0) s_prefix = e;
+    }
     __syncthreads();
     const unsigned prefix = s_prefix;
 #pragma unroll
@@ -1009,15 +1026,18 @@ __global__ void __launch_bounds__(kSchedThreads) k_sched(SimConst c, const uint8
     for (int o = 16; o > 0; o >>= 1) wt += __shfl_xor_sync(0xffffffffu, wt, o);
     if (lane == 0) s_wtot[warp] = wt;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        int run = 0;
-        for (int w = 0; w < kSchedThreads / 32; w++) {
-            s_wbase[w] = run;
-            run += s_wtot[w];
+    if (warp == 0) {
+        int tot = 0;
+        for (int w = 0; w < kSchedThreads / 32; w++) tot += s_wtot[w];
+        const unsigned prefix = lookback_publish_warp(lb, epoch, tile, (unsigned)tot);
+        if (lane == 0) {
+            int run = (int)prefix;
+            for (int w = 0; w < kSchedThreads / 32; w++) {
+                s_wbase[w] = run;
+                run += s_wtot[w];
+            }
+            if (tile == (int)gridDim.x - 1) sc->marked_entries = run;
         }
-        const unsigned prefix = lookback_publish(lb, epoch, tile, (unsigned)run);
-        for (int w = 0; w < kSchedThreads / 32; w++) s_wbase[w] += (int)prefix;
-        if (tile == (int)gridDim.x - 1) sc->marked_entries = (int)prefix + run;
     }
     __syncthreads();
     // append the marked entries, rounds in order, lanes in order within a round
