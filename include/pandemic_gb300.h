@@ -185,6 +185,67 @@ void pt_destroy(pt_sim *sim);
 /* Text of the last error on sim (or of the last failed pt_create when sim is NULL). */
 const char *pt_last_error(const pt_sim *sim);
 
+/* ------------------------------------------------------------------ batches
+ * A batch runs many independent simulations (replicates, scenarios, uneven sizes)
+ * together: every day is one set of kernel launches over all of them, and the whole
+ * day loop is one CUDA graph.  The reference runs one simulation per process; its
+ * PythonBatcher scripts (write_gpu_constants.py) start one process per scenario and
+ * seed.  Instance k of a batch gives exactly the results of pt_create(&params[k],
+ * core_seeds[k]) run alone: statistics rows, generation counts and per-person state.
+ * A pt_batch is not thread-safe and runs on one CUDA stream. */
+typedef struct pt_batch pt_batch;
+
+#define PT_BATCH_MAX_INSTANCES 4096
+
+/* instances simulations, params[k] and core_seeds[k] each as pt_create takes them. */
+pt_status pt_batch_create(const pt_params *params, const int *core_seeds, int instances, void *cuda_stream,
+                          pt_batch **out);
+
+/* setupSim of every instance, each in its own region of the batch's arrays. */
+pt_status pt_batch_setup(pt_batch *batch);
+
+/* Runs every instance to completion (its zero-infected day or max_days) and copies
+ * the per-day results back; read them with pt_batch_counts. */
+pt_status pt_batch_run(pt_batch *batch);
+
+/* One day of every instance still running.  running (may be NULL) receives the
+ * number of instances still running after the day.  Returns PT_DONE once no instance
+ * has infected left, PT_FINISHED once the longest max_days has run. */
+pt_status pt_batch_step_day(pt_batch *batch, int *running);
+
+pt_status pt_batch_reset_epidemic(pt_batch *batch);
+
+/* Instance count, real persons over all instances and persons including the padding
+ * that starts each instance on a 4096-person boundary. */
+pt_status pt_batch_size(const pt_batch *batch, int *instances, int64_t *persons, int64_t *padded_persons);
+
+/* Results of one instance as pt_run returns them (any pointer may be NULL). */
+pt_status pt_batch_counts(const pt_batch *batch, int instance, int *counts, int *infected, int *days_run);
+
+/* final_countReproduction of every instance: instances x 256 ints per strain. */
+pt_status pt_batch_final_gen_counts(pt_batch *batch, int *gen_p, int *gen_s);
+
+pt_status pt_batch_get_info(const pt_batch *batch, int instance, pt_info *out);
+
+/* pt_get_person_state and pt_get_population of one instance, in its own numbering
+ * (person, household and location ids as the instance run alone has them). */
+pt_status pt_batch_get_person_state(pt_batch *batch, int instance, uint8_t *status_p, uint8_t *status_s,
+                                    uint8_t *day_p, uint8_t *day_s, uint8_t *gen_p, uint8_t *gen_s,
+                                    uint8_t *age);
+pt_status pt_batch_get_population(pt_batch *batch, int instance, int32_t *household, int32_t *household_offset,
+                                  int32_t *workplace, int32_t *workplace_people, int32_t *workplace_offset);
+
+/* As pt_set_timing / pt_get_stage_ms, for the batch's days. */
+pt_status pt_batch_set_timing(pt_batch *batch, int enabled);
+pt_status pt_batch_get_stage_ms(pt_batch *batch, float ms[16], int days[2]);
+
+pt_status pt_batch_transfer_bytes(const pt_batch *batch, uint64_t *h2d, uint64_t *d2h);
+
+void pt_batch_destroy(pt_batch *batch);
+
+/* Text of the last error on batch (or of the last failed pt_batch_create when NULL). */
+const char *pt_batch_last_error(const pt_batch *batch);
+
 #ifdef __cplusplus
 }
 #endif

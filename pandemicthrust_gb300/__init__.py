@@ -17,8 +17,8 @@ import numpy as np
 
 from .build import build as _build, LIB as LIBRARY_PATH, CLI as CLI_PATH
 
-__all__ = ["PandemicSim", "Params", "load_library", "build", "PtError", "LIBRARY_PATH", "CLI_PATH",
-           "PT_OK", "PT_DONE", "PT_FINISHED"]
+__all__ = ["PandemicSim", "PandemicBatch", "Params", "load_library", "build", "PtError", "LIBRARY_PATH",
+           "CLI_PATH", "PT_OK", "PT_DONE", "PT_FINISHED"]
 
 PT_OK, PT_DONE, PT_FINISHED = 0, 1, 2
 _STATUS = {0: "PT_OK", 1: "PT_DONE", 2: "PT_FINISHED", -1: "PT_ERR_ARG", -2: "PT_ERR_IO", -3: "PT_ERR_PARSE",
@@ -73,6 +73,10 @@ EXPORTS = [
     "pt_final_gen_counts", "pt_reset_epidemic", "pt_get_info", "pt_get_person_state",
     "pt_get_population", "pt_get_day_tables", "pt_set_full_tables", "pt_set_timing", "pt_get_stage_ms",
     "pt_launch_count", "pt_transfer_bytes", "pt_destroy", "pt_last_error",
+    "pt_batch_create", "pt_batch_setup", "pt_batch_run", "pt_batch_step_day", "pt_batch_reset_epidemic",
+    "pt_batch_size", "pt_batch_counts", "pt_batch_final_gen_counts", "pt_batch_get_info",
+    "pt_batch_get_person_state", "pt_batch_get_population", "pt_batch_set_timing", "pt_batch_get_stage_ms",
+    "pt_batch_transfer_bytes", "pt_batch_destroy", "pt_batch_last_error",
 ]
 
 _lib = None
@@ -114,6 +118,24 @@ def load_library(path=None):
     lib.pt_destroy.argtypes = [vp]
     lib.pt_last_error.argtypes = [vp]
     lib.pt_last_error.restype = ctypes.c_char_p
+    i64p, u64p = ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_uint64)
+    lib.pt_batch_create.argtypes = [ctypes.POINTER(Params), ip, ctypes.c_int, vp, ctypes.POINTER(vp)]
+    lib.pt_batch_setup.argtypes = [vp]
+    lib.pt_batch_run.argtypes = [vp]
+    lib.pt_batch_step_day.argtypes = [vp, ip]
+    lib.pt_batch_reset_epidemic.argtypes = [vp]
+    lib.pt_batch_size.argtypes = [vp, ip, i64p, i64p]
+    lib.pt_batch_counts.argtypes = [vp, ctypes.c_int, ip, ip, ip]
+    lib.pt_batch_final_gen_counts.argtypes = [vp, ip, ip]
+    lib.pt_batch_get_info.argtypes = [vp, ctypes.c_int, ctypes.POINTER(Info)]
+    lib.pt_batch_get_person_state.argtypes = [vp, ctypes.c_int] + [u8p] * 7
+    lib.pt_batch_get_population.argtypes = [vp, ctypes.c_int] + [i32p] * 5
+    lib.pt_batch_set_timing.argtypes = [vp, ctypes.c_int]
+    lib.pt_batch_get_stage_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ip]
+    lib.pt_batch_transfer_bytes.argtypes = [vp, u64p, u64p]
+    lib.pt_batch_destroy.argtypes = [vp]
+    lib.pt_batch_last_error.argtypes = [vp]
+    lib.pt_batch_last_error.restype = ctypes.c_char_p
     if path == LIBRARY_PATH:
         _lib = lib
     return lib
@@ -150,8 +172,7 @@ class PandemicSim:
     def info(self):
         i = Info()
         self._check(self.lib.pt_get_info(self.h, ctypes.byref(i)))
-        return {name: (list(getattr(i, name)) if hasattr(getattr(i, name), "__len__") else getattr(i, name))
-                for name, _ in Info._fields_}
+        return _info_dict(i)
 
     def step_day(self):
         """One day: returns (status, counts16, infected_count)."""
@@ -237,6 +258,144 @@ class PandemicSim:
     def close(self):
         if getattr(self, "h", None):
             self.lib.pt_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _info_dict(i):
+    return {name: (list(getattr(i, name)) if hasattr(getattr(i, name), "__len__") else getattr(i, name))
+            for name, _ in Info._fields_}
+
+
+class PandemicBatch:
+    """Many independent simulations advanced together on the current CUDA device.
+
+    Instance k gives exactly what ``PandemicSim(params[k], core_seeds[k])`` gives run
+    alone.  The reference runs one process per scenario and seed (its PythonBatcher
+    scripts); here every day is one set of launches over all instances and the day
+    loop is one CUDA graph.
+    """
+
+    def __init__(self, params, core_seeds, stream=None):
+        self.lib = load_library()
+        params = [Params.from_dict(p) if isinstance(p, dict) else p for p in params]
+        if len(params) != len(core_seeds):
+            raise ValueError("one core seed per instance")
+        self.k = len(params)
+        self.params = params
+        arr = (Params * self.k)(*params)
+        seeds = (ctypes.c_int * self.k)(*[int(x) for x in core_seeds])
+        h = ctypes.c_void_p()
+        rc = self.lib.pt_batch_create(arr, seeds, self.k, stream, ctypes.byref(h))
+        if rc != PT_OK:
+            raise PtError(rc, self.lib.pt_batch_last_error(None).decode())
+        self.h = h
+
+    def _check(self, rc, ok=(PT_OK,)):
+        if rc not in ok:
+            raise PtError(rc, self.lib.pt_batch_last_error(self.h).decode())
+        return rc
+
+    def setup(self):
+        self._check(self.lib.pt_batch_setup(self.h))
+
+    def run(self):
+        """Every instance to completion."""
+        self._check(self.lib.pt_batch_run(self.h))
+
+    def step_day(self):
+        """One day of every running instance: (status, instances still running)."""
+        n = ctypes.c_int(0)
+        rc = self._check(self.lib.pt_batch_step_day(self.h, ctypes.byref(n)), ok=(PT_OK, PT_DONE, PT_FINISHED))
+        return rc, n.value
+
+    def reset_epidemic(self):
+        self._check(self.lib.pt_batch_reset_epidemic(self.h))
+
+    def size(self):
+        """(instances, persons, persons including padding)."""
+        k, n, p = ctypes.c_int(0), ctypes.c_int64(0), ctypes.c_int64(0)
+        self._check(self.lib.pt_batch_size(self.h, ctypes.byref(k), ctypes.byref(n), ctypes.byref(p)))
+        return k.value, n.value, p.value
+
+    def counts(self, k):
+        """(counts [days, 16], infected [days]) of instance k, as PandemicSim.runToCompletion."""
+        counts = np.zeros((256, 16), dtype=np.int32)
+        infected = np.zeros(256, dtype=np.int32)
+        rows = ctypes.c_int(0)
+        self._check(self.lib.pt_batch_counts(self.h, k, _ptr(counts, ctypes.c_int), _ptr(infected, ctypes.c_int),
+                                             ctypes.byref(rows)))
+        return counts[:rows.value].copy(), infected[:rows.value].copy()
+
+    def days_run(self):
+        """Statistics rows of every instance."""
+        out = np.zeros(self.k, dtype=np.int64)
+        for k in range(self.k):
+            rows = ctypes.c_int(0)
+            self._check(self.lib.pt_batch_counts(self.h, k, None, None, ctypes.byref(rows)))
+            out[k] = rows.value
+        return out
+
+    def final_gen_counts(self):
+        """(gen_p, gen_s), each [instances, 256]."""
+        gp = np.zeros((self.k, 256), dtype=np.int32)
+        gs = np.zeros((self.k, 256), dtype=np.int32)
+        self._check(self.lib.pt_batch_final_gen_counts(self.h, _ptr(gp, ctypes.c_int), _ptr(gs, ctypes.c_int)))
+        return gp, gs
+
+    def info(self, k):
+        i = Info()
+        self._check(self.lib.pt_batch_get_info(self.h, k, ctypes.byref(i)))
+        return _info_dict(i)
+
+    def person_state(self, k):
+        n = self.info(k)["number_people"]
+        names = ("status_p", "status_s", "day_p", "day_s", "gen_p", "gen_s", "age")
+        out = {name: np.zeros(n, dtype=np.uint8) for name in names}
+        self._check(self.lib.pt_batch_get_person_state(self.h, k, *[_ptr(out[name], ctypes.c_uint8) for name in names]))
+        return out
+
+    def population(self, k):
+        i = self.info(k)
+        N, H, L = i["number_people"], i["number_households"], i["number_workplaces"]
+        out = dict(household=np.zeros(N, np.int32), household_offset=np.zeros(H + 1, np.int32),
+                   workplace=np.zeros(N, np.int32), workplace_people=np.zeros(N, np.int32),
+                   workplace_offset=np.zeros(L + 1, np.int32))
+        self._check(self.lib.pt_batch_get_population(self.h, k, *[_ptr(out[n], ctypes.c_int32) for n in
+                                                                   ("household", "household_offset", "workplace",
+                                                                    "workplace_people", "workplace_offset")]))
+        return out
+
+    def set_timing(self, on=True):
+        self._check(self.lib.pt_batch_set_timing(self.h, 1 if on else 0))
+
+    def stage_ms(self):
+        a = (ctypes.c_float * 16)()
+        days = (ctypes.c_int * 2)()
+        self._check(self.lib.pt_batch_get_stage_ms(self.h, a, days))
+        out = {"weekday": {n: a[k] for k, n in enumerate(PandemicSim.STAGES)},
+               "weekend": {n: a[8 + k] for k, n in enumerate(PandemicSim.STAGES)}}
+        return out, (days[0], days[1])
+
+    def transfer_bytes(self):
+        a, b = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        self._check(self.lib.pt_batch_transfer_bytes(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pt_batch_destroy(self.h)
             self.h = None
 
     def __enter__(self):

@@ -13,22 +13,22 @@ namespace ptk {
 
 // ---------------------------------------------------------------- tables
 // PandemicSim.cu:328-481 (model constants; identical in every simulation).
-__constant__ float c_child_age_cdf[5] = {0.24f, 0.47f, 0.72f, 0.85f, 1.0f};
-__constant__ float c_workplace_pdf[kTypes] = {
+static __constant__ float c_child_age_cdf[5] = {0.24f, 0.47f, 0.72f, 0.85f, 1.0f};
+static __constant__ float c_workplace_pdf[kTypes] = {
     0.06586f, 0.05802f, 0.30227f, 0.0048f, 0.00997f, 0.203f, 0.09736f,
     0.10598f, 0.00681f, 0.02599f, 0.f, 0.08749f, 0.03181f, 0.00064f};
-__constant__ int c_type_max_contacts[kTypes] = {3, 3, 3, 2, 2, 3, 3, 2, 2, 2, 0, 2, 2, 2};
-__constant__ float c_weekday_errand_pdf[kTypes] = {0, 0, 0, 0, 0, 0, 0, 0, 0,
+static __constant__ int c_type_max_contacts[kTypes] = {3, 3, 3, 2, 2, 3, 3, 2, 2, 2, 0, 2, 2, 2};
+static __constant__ float c_weekday_errand_pdf[kTypes] = {0, 0, 0, 0, 0, 0, 0, 0, 0,
                                                    0.61919f, 0, 0.27812f, 0.06601f, 0.03668f};
-__constant__ float c_weekend_errand_pdf[kTypes] = {0, 0, 0, 0, 0, 0, 0, 0, 0,
+static __constant__ float c_weekend_errand_pdf[kTypes] = {0, 0, 0, 0, 0, 0, 0, 0, 0,
                                                    0.51493f, 0, 0.25586f, 0.1162f, 0.113f};
-__constant__ int c_hh_adults[9] = {1, 1, 2, 1, 2, 1, 2, 1, 2};
-__constant__ int c_hh_children[9] = {0, 1, 0, 2, 1, 3, 2, 4, 3};
-__constant__ float c_hh_cdf[9] = {0.279f, 0.319f, 0.628f, 0.671f, 0.8f, 0.812f, 0.939f, 0.944f, 1.0f};
+static __constant__ int c_hh_adults[9] = {1, 1, 2, 1, 2, 1, 2, 1, 2};
+static __constant__ int c_hh_children[9] = {0, 1, 0, 2, 1, 3, 2, 4, 3};
+static __constant__ float c_hh_cdf[9] = {0.279f, 0.319f, 0.628f, 0.671f, 0.8f, 0.812f, 0.939f, 0.944f, 1.0f};
 // Contacts per errand hour for weekday profiles 0..3 (3 = afterschool) and the
 // errand slot of each of the two weekend errand contacts (PandemicSim.cu:445-481).
-__constant__ int c_weekday_assign[4][2] = {{2, 0}, {0, 2}, {1, 1}, {2, 0}};
-__constant__ int c_weekend_assign[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+static __constant__ int c_weekday_assign[4][2] = {{2, 0}, {0, 2}, {1, 1}, {2, 0}};
+static __constant__ int c_weekend_assign[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
 
 // ---------------------------------------------------------------- Threefry
 // Threefry-2x64-20 and 2x32-20 (Salmon et al., SC'11; the Random123 rotation

@@ -20,6 +20,7 @@
 #include <atomic>
 #include "pt_kernels.h"
 #include "pt_device.cuh"
+#include "pt_lookback.cuh"
 
 namespace ptk {
 
@@ -42,136 +43,14 @@ int sm_count()
 
 static inline int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
 
-constexpr long long kSpinLimit = 1ll << 22;
-
-// ------------------------------------------------------------------ look-back
-// Tile status word: bits 63..34 epoch, 33..32 flag (1 aggregate, 2 inclusive
-// prefix), 31..0 value.  The epoch makes words of earlier launches stale without a
-// memset: the last block to finish a launch increments it and resets the tickets.
-struct LookBack {
-    unsigned long long *tiles;
-    int *ctl;   // ctl[0] ticket, ctl[1] finished, ctl[2] epoch
-    int *error;
-};
-
-__device__ __forceinline__ unsigned long long lb_word(unsigned epoch, unsigned flag, unsigned value)
-{
-    return ((unsigned long long)epoch << 34) | ((unsigned long long)flag << 32) | value;
-}
-
-// Called by all 32 lanes of one warp.  Publishes the tile aggregate, then walks back
-// 32 predecessors per step (one word per lane) to the nearest inclusive prefix,
-// publishes the tile's inclusive prefix and returns the exclusive one on every lane.
-__device__ unsigned lookback_publish_warp(const LookBack &lb, unsigned epoch, int tile, unsigned aggregate)
-{
-    volatile unsigned long long *t = lb.tiles;
-    const int lane = threadIdx.x & 31;
-    if (tile == 0) {
-        if (lane == 0) t[0] = lb_word(epoch, 2, aggregate);
-        return 0;
-    }
-    if (lane == 0) t[tile] = lb_word(epoch, 1, aggregate);
-    unsigned excl = 0;
-    int top = tile - 1;  // the window covers tiles top, top-1, ..., top-31
-    long long spins = 0;
-    while (true) {
-        const int j = top - lane;
-        unsigned long long w = j >= 0 ? t[j] : lb_word(epoch, 2, 0);  // before tile 0: prefix 0
-        const bool ready = (unsigned)(w >> 34) == (epoch & 0x3FFFFFFFu) && ((unsigned)(w >> 32) & 3u) != 0;
-        const bool prefix = ready && ((unsigned)(w >> 32) & 3u) == 2;
-        const unsigned rmask = __ballot_sync(0xffffffffu, ready);
-        const unsigned pmask = __ballot_sync(0xffffffffu, prefix);
-        // lanes up to (and including) the closest prefix must all be ready
-        const int stop = pmask ? __ffs(pmask) - 1 : 31;
-        const unsigned need = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
-        if ((rmask & need) == need) {
-            unsigned v = (lane <= stop) ? (unsigned)w : 0u;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            excl += v;
-            if (pmask) break;
-            top -= 32;
-            continue;
-        }
-        if (++spins > kSpinLimit) {
-            if (lane == 0) atomicExch(lb.error, 1);
-            break;
-        }
-        __nanosleep(64);
-    }
-    if (lane == 0) t[tile] = lb_word(epoch, 2, excl + aggregate);
-    return excl;
-}
-
-// Start of a look-back launch: returns the tile index and epoch (broadcast).
-__device__ __forceinline__ void lookback_begin(const LookBack &lb, int &tile, unsigned &epoch)
-{
-    __shared__ int s_tile;
-    __shared__ unsigned s_epoch;
-    if (threadIdx.x == 0) {
-        s_tile = atomicAdd(&lb.ctl[0], 1);
-        s_epoch = (unsigned)(*(volatile int *)&lb.ctl[2]) & 0x3FFFFFFFu;
-    }
-    __syncthreads();
-    tile = s_tile;
-    epoch = s_epoch;
-}
-
-// End of a look-back launch: the last block resets the ticket and bumps the epoch.
-__device__ __forceinline__ void lookback_end(const LookBack &lb)
-{
-    if (threadIdx.x == 0) {
-        __threadfence();
-        int fin = atomicAdd(&lb.ctl[1], 1);
-        if (fin == (int)gridDim.x - 1) {
-            lb.ctl[0] = 0;
-            lb.ctl[1] = 0;
-            atomicAdd(&lb.ctl[2], 1);
-            __threadfence();
-        }
-    }
-}
-
-// ------------------------------------------------------------------ block scan
-template <int THREADS, typename T>
-__device__ __forceinline__ T block_exclusive_scan(T v, T &total)
-{
-    static_assert(THREADS % 32 == 0, "");
-    constexpr int W = THREADS / 32;
-    __shared__ T s_warp[W];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    T x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        T y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) s_warp[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        T w = lane < W ? s_warp[lane] : T(0);
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            T y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += y;
-        }
-        if (lane < W) s_warp[lane] = w;
-    }
-    __syncthreads();
-    T warp_prefix = warp > 0 ? s_warp[warp - 1] : T(0);
-    total = s_warp[W - 1];
-    __syncthreads();
-    return warp_prefix + x - v;
-}
-
 // ================================================================== setup
 // kernel_householdTypeAssignment + hh_peopleCount_functor (PandemicSim.cu:2329-2357,
 // :3579-3605): counter g -> households 4g..4g+3.  Writes each household's size and
-// counts adults.
-__global__ void k_household_types(SimConst c, uint8_t *types, int32_t *sizes, int *adults)
+// counts adults and persons.
+__global__ void k_household_types(SimConst c, uint8_t *types, int32_t *sizes, int *adults, int *persons)
 {
     const TfKey key = make_key(c);
-    int local_adults = 0;
+    int local_adults = 0, local_persons = 0;
     const int G = c.H / 4;
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x) {
         uint32_t w[4];
@@ -184,20 +63,25 @@ __global__ void k_household_types(SimConst c, uint8_t *types, int32_t *sizes, in
                 types[h] = (uint8_t)t;
                 sizes[h] = c_hh_adults[t] + c_hh_children[t];
                 local_adults += c_hh_adults[t];
+                local_persons += c_hh_adults[t] + c_hh_children[t];
             }
         }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) local_adults += __shfl_xor_sync(0xffffffffu, local_adults, o);
+    for (int o = 16; o > 0; o >>= 1) {
+        local_adults += __shfl_xor_sync(0xffffffffu, local_adults, o);
+        local_persons += __shfl_xor_sync(0xffffffffu, local_persons, o);
+    }
     if ((threadIdx.x & 31) == 0 && local_adults) atomicAdd(adults, local_adults);
+    if ((threadIdx.x & 31) == 0 && local_persons) atomicAdd(persons, local_persons);
 }
 
-cudaError_t launch_household_types(const SimConst &c, uint8_t *types, int32_t *sizes, int *adults,
+cudaError_t launch_household_types(const SimConst &c, uint8_t *types, int32_t *sizes, int *adults, int *persons,
                                    cudaStream_t s)
 {
     int G = c.H / 4 + 1;
     int blocks = std::min(div_up(G, 256), sm_count() * 16);
-    k_household_types<<<blocks, 256, 0, s>>>(c, types, sizes, adults);
+    k_household_types<<<blocks, 256, 0, s>>>(c, types, sizes, adults, persons);
     count_launch();
     return cudaGetLastError();
 }
@@ -279,16 +163,6 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *in, int32_
     lookback_end(lb);
 }
 
-// The look-back control block sits right after the tile words.
-static LookBack make_lb(unsigned long long *tiles, int tiles_cap, int *error)
-{
-    LookBack lb;
-    lb.tiles = tiles;
-    lb.ctl = (int *)(tiles + tiles_cap);
-    lb.error = error;
-    return lb;
-}
-
 cudaError_t launch_scan_exclusive(const int32_t *in, int32_t *out, int n, int clear_in,
                                   unsigned long long *tiles, int *ctl, int *error,
                                   const int *skip, int passes, int *digit_hist, cudaStream_t s,
@@ -320,12 +194,14 @@ __global__ void k_digit_bases(int *digit_hist, int *digit_base, int passes, cons
 }
 
 // kernel_generateHouseholds (PandemicSim.cu:2490-2531): adults first (AGE_ADULT),
-// then children with the AGE_5 placeholder.
-__global__ void k_generate_households(SimConst c, const uint8_t *types, const int32_t *hh_offset,
-                                      int32_t *household, uint8_t *age)
+// then children with the AGE_5 placeholder.  Slots of type 0xFF hold an instance's
+// padding persons and are skipped.
+__global__ void k_generate_households(const uint8_t *types, const int32_t *hh_offset, int slots, int32_t *household,
+                                      uint8_t *age)
 {
-    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < c.H; h += gridDim.x * blockDim.x) {
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < slots; h += gridDim.x * blockDim.x) {
         int t = types[h];
+        if (t > 8) continue;
         int off = hh_offset[h];
         int na = c_hh_adults[t], nc = c_hh_children[t];
         for (int i = 0; i < na + nc; i++) {
@@ -335,18 +211,19 @@ __global__ void k_generate_households(SimConst c, const uint8_t *types, const in
     }
 }
 
-cudaError_t launch_generate_households(const SimConst &c, const uint8_t *types, const int32_t *hh_offset,
-                                       int32_t *household, uint8_t *age, cudaStream_t s)
+cudaError_t launch_generate_households(const uint8_t *types, const int32_t *hh_offset, int slots, int32_t *household,
+                                       uint8_t *age, cudaStream_t s)
 {
-    int blocks = std::min(div_up(c.H, 256), sm_count() * 16);
-    k_generate_households<<<blocks, 256, 0, s>>>(c, types, hh_offset, household, age);
+    int blocks = std::max(1, std::min(div_up(slots, 256), sm_count() * 16));
+    k_generate_households<<<blocks, 256, 0, s>>>(types, hh_offset, slots, household, age);
     count_launch();
     return cudaGetLastError();
 }
 
 // assignWorkplaceFunctor (PandemicSim.cu:3750-3778): counter W0 + g -> persons
-// 4g..4g+3; adults draw a workplace, children an age band and school.
-__global__ void k_assign_workplaces(SimConst c, uint8_t *age, int32_t *workplace)
+// 4g..4g+3; adults draw a workplace, children an age band and school.  loc_base turns
+// the instance's location number into a global one.
+__global__ void k_assign_workplaces(SimConst c, uint8_t *age, int32_t *workplace, int loc_base)
 {
     const TfKey key = make_key(c);
     const int G = c.N / 4;
@@ -359,9 +236,9 @@ __global__ void k_assign_workplaces(SimConst c, uint8_t *age, int32_t *workplace
             if (p < c.N) {
                 int a = age[p];
                 if (a == 5) {
-                    workplace[p] = fish_workplace(c, w[i]);
+                    workplace[p] = loc_base + fish_workplace(c, w[i]);
                 } else {
-                    workplace[p] = fish_school_and_age(c, w[i], &a);
+                    workplace[p] = loc_base + fish_school_and_age(c, w[i], &a);
                     age[p] = (uint8_t)a;
                 }
             }
@@ -369,10 +246,46 @@ __global__ void k_assign_workplaces(SimConst c, uint8_t *age, int32_t *workplace
     }
 }
 
-cudaError_t launch_assign_workplaces(const SimConst &c, uint8_t *age, int32_t *workplace, cudaStream_t s)
+cudaError_t launch_assign_workplaces(const SimConst &c, uint8_t *age, int32_t *workplace, int loc_base, cudaStream_t s)
 {
     int blocks = std::min(div_up(c.N / 4 + 1, 256), sm_count() * 16);
-    k_assign_workplaces<<<blocks, 256, 0, s>>>(c, age, workplace);
+    k_assign_workplaces<<<blocks, 256, 0, s>>>(c, age, workplace, loc_base);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// Padding of a batch, one block per instance.  Without `persons`: the instance's
+// last household slot gets type 0xFF and the padding count as its size, so one scan
+// of all slots yields tile-aligned person bases.  With `persons`: the padding persons
+// get no household, no age and the spare location, which sorts them behind every
+// real workplace.
+__global__ void k_batch_padding(const InstConst *ic, int K, int P, uint8_t *types, int32_t *sizes,
+                                int32_t *household, uint8_t *age, int32_t *workplace, int spare, int persons)
+{
+    const int k = blockIdx.x;
+    if (k >= K) return;
+    const InstConst &c = ic[k];
+    const int end = k + 1 < K ? ic[k + 1].pbase : P;
+    const int first = c.pbase + c.c.N;
+    if (!persons) {
+        if (threadIdx.x == 0) {
+            types[c.hbase + c.c.H] = 0xFF;
+            sizes[c.hbase + c.c.H] = end - first;
+        }
+        return;
+    }
+    for (int p = first + threadIdx.x; p < end; p += blockDim.x) {
+        household[p] = -1;
+        age[p] = 0;
+        workplace[p] = spare;
+    }
+}
+
+cudaError_t launch_batch_padding(const DevArrays &d, uint8_t *types, int32_t *sizes, int spare_location, bool persons,
+                                 cudaStream_t s)
+{
+    k_batch_padding<<<d.K, 256, 0, s>>>(d.ic, d.K, d.P, types, sizes, d.household, d.age, d.workplace,
+                                        spare_location, persons ? 1 : 0);
     count_launch();
     return cudaGetLastError();
 }
@@ -679,6 +592,25 @@ cudaError_t launch_init_status(int N, uint32_t *state, uint8_t *gen_p, uint8_t *
     return cudaGetLastError();
 }
 
+// One block per instance: zero its state words, then set the counter offset.
+__global__ void k_reset_instances(const InstConst *ic, InstState *is, int K)
+{
+    const int k = blockIdx.x;
+    if (k >= K) return;
+    int *w = reinterpret_cast<int *>(&is[k]);
+    for (int i = threadIdx.x; i < (int)(sizeof(InstState) / 4); i += blockDim.x) w[i] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        is[k].rand_offset = (unsigned long long)(ic[k].c.H / 4) + (unsigned long long)(ic[k].c.N / 4);
+}
+
+cudaError_t launch_reset_instances(const DevArrays &d, cudaStream_t s)
+{
+    k_reset_instances<<<d.K, 256, 0, s>>>(d.ic, d.is, d.K);
+    count_launch();
+    return cudaGetLastError();
+}
+
 // setup_initialInfected (PandemicSim.cu:708-758): the first P seeds get the pandemic
 // strain, the next S the seasonal one; status STATUS_INFECTED, day 0, generation 0.
 __global__ void k_seed_infected(const int32_t *seeds, int P, int S, uint32_t *state, uint8_t *gen_p, uint8_t *gen_s)
@@ -705,10 +637,22 @@ cudaError_t launch_seed_infected(const int32_t *seeds, int P, int S, uint32_t *s
 }
 
 // ================================================================== day
+// Every day kernel covers all instances of a batch in one launch.  Persons are
+// global ids; a person tile (kPersonTile persons) belongs to one instance
+// (tile_inst), and an infected list position to the instance in infected_inst.
+
+// An instance takes part in a day until a day counts zero infected, and for at
+// most its max_days days.
+__device__ __forceinline__ bool instance_running(const InstConst &c, const InstState &s, int day)
+{
+    return !s.done && day < c.max_days;
+}
+
 // Sweep: one tile of 4096 persons per block; each thread holds 4 rounds of 4
 // persons (one 16-byte load per round).  Output order is (round, thread, item),
 // which is ascending person order within the tile.
 constexpr int kSweepThreads = 256, kSweepRounds = 4, kSweepTile = kSweepThreads * 4 * kSweepRounds;
+static_assert(kSweepTile == kPersonTile, "a sweep tile is a person tile");
 
 constexpr uint32_t kNeverInfected = 0x01u | (0x01u << 8) | (0xFFu << 16) | (0xFFu << 24);
 
@@ -722,16 +666,69 @@ __device__ __forceinline__ uint32_t recover_word(uint32_t st, int d2r, bool &cha
     return out;
 }
 
-__global__ void __launch_bounds__(kSweepThreads) k_sweep(SimConst c, uint32_t *state, int32_t *infected,
-                                                         Scalars *sc, LookBack lb, int day)
+// End of the sweep, run by the last block to finish: each running instance's day
+// bookkeeping (runToCompletion, PandemicSim.cu:891-937: the statistics row, the stop
+// on zero infected, the counter offsets E0 / R0 of the schedule and the contacts),
+// and the start of each instance's run of the infected list.
+__device__ void sweep_day_end(const InstConst *ic, InstState *is, int K, Scalars *sc, int day)
+{
+    const bool weekend = (day % 7) >= 5;  // PandemicSim.h:283-284
+    int carry = 0;
+    for (int b = 0; b < K; b += kSweepThreads) {
+        const int k = b + (int)threadIdx.x;
+        int I = 0;
+        if (k < K) {
+            InstState &s = is[k];
+            const int counted = atomicExch(&s.tile_infected, 0);
+            if (instance_running(ic[k], s, day)) {
+                I = counted;
+                s.infected = I;
+                s.infected_per_day[day] = I;
+                s.day = day;
+                s.days_run = day + 1;
+                if (I == 0) {
+                    s.done = 1;
+                } else {
+                    const unsigned long long N = (unsigned long long)ic[k].c.N;
+                    const unsigned long long E0 = s.rand_offset;
+                    const unsigned long long R0 = E0 + (weekend ? 2ull * N : N / 2ull);
+                    s.errand_offset = E0;
+                    s.infect_offset = R0;
+                    s.rand_offset = R0 + 6ull * (unsigned long long)I;
+                }
+            } else {
+                s.infected = 0;
+            }
+        }
+        int total;
+        const int excl = block_exclusive_scan<kSweepThreads, int>(I, total);
+        if (k < K) is[k].start = carry + excl;
+        carry += total;
+    }
+    if (threadIdx.x == 0) {
+        sc->infected = carry;
+        sc->day = day;
+        sc->new_count = 0;
+        if (carry == 0) sc->done = 1;
+    }
+}
+
+// kernel_countInfectedStatusAndRecover (PandemicSim.cu:2097-2192) and the copy_if
+// of the infected (:2207-2224) in one pass: recover, count the 16 status bins of the
+// instance, and write the ascending infected list by a decoupled look-back.
+__global__ void __launch_bounds__(kSweepThreads) k_sweep(const InstConst *ic, InstState *is, const int32_t *tile_inst,
+                                                         int K, uint32_t *state, int32_t *infected,
+                                                         int32_t *infected_inst, Scalars *sc, LookBack lb, int day)
 {
     if (*(volatile int *)&sc->done) return;
     int tile;
     unsigned epoch;
     lookback_begin(lb, tile, epoch);
-    const int N = c.N;
-    const int d2r = day - 10;
+    const int k = tile_inst[tile];
     const long long tile_base = (long long)tile * kSweepTile;
+    // end of the tile's persons: none when the instance no longer runs
+    const long long N = instance_running(ic[k], is[k], day) ? (long long)ic[k].pbase + ic[k].c.N : tile_base;
+    const int d2r = day - 10;
     // packed per-thread status bins: 16-bit fields, bins 0-3 / 4-7 per strain
     unsigned long long bp_lo = 0, bp_hi = 0, bs_lo = 0, bs_hi = 0;
     int nss = 0;         // persons in the never-infected state (S, S, day 255, day 255)
@@ -830,46 +827,58 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(SimConst c, uint32_t *s
         long long p0 = tile_base + ((long long)r * kSweepThreads + threadIdx.x) * 4;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            if (flags & (1u << (4 * r + j))) infected[pos++] = (int32_t)(p0 + j);
+            if (flags & (1u << (4 * r + j))) {
+                infected[pos] = (int32_t)(p0 + j);
+                infected_inst[pos] = k;
+                pos++;
+            }
         }
     }
-    if (threadIdx.x < 16 && s_bins[threadIdx.x]) atomicAdd(&sc->counts[day][threadIdx.x], s_bins[threadIdx.x]);
-    // the last tile closes the day's bookkeeping (runToCompletion, PandemicSim.cu:891-937)
-    if (tile == (int)gridDim.x - 1 && threadIdx.x == 0) {
-        const int I = (int)(prefix + tile_total);
-        sc->infected = I;
-        sc->infected_per_day[day] = I;
-        sc->day = day;
-        sc->days_run = day + 1;
-        sc->new_count = 0;
-        if (I == 0) {
-            sc->done = 1;
-        } else {
-            const bool weekend = (day % 7) >= 5;
-            unsigned long long E0 = sc->rand_offset;
-            unsigned long long R0 = E0 + (weekend ? 2ull * (unsigned long long)N : (unsigned long long)(N / 2));
-            sc->errand_offset = E0;
-            sc->infect_offset = R0;
-            sc->rand_offset = R0 + 6ull * (unsigned long long)I;
-        }
+    if (threadIdx.x < 16 && s_bins[threadIdx.x]) atomicAdd(&is[k].counts[day][threadIdx.x], s_bins[threadIdx.x]);
+    if (threadIdx.x == 0 && tile_total) atomicAdd(&is[k].tile_infected, (int)tile_total);
+    // the last block to finish closes the day of every instance
+    __threadfence();
+    __syncthreads();
+    __shared__ int s_last;
+    if (threadIdx.x == 0) s_last = atomicAdd(&lb.ctl[1], 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    sweep_day_end(ic, is, K, sc, day);
+    if (threadIdx.x == 0) {
+        lb.ctl[0] = 0;
+        lb.ctl[1] = 0;
+        atomicAdd(&lb.ctl[2], 1);
+        __threadfence();
     }
-    lookback_end(lb);
 }
 
-cudaError_t launch_sweep(const SimConst &c, const DevArrays &d, int day, cudaStream_t s)
+// The look-back control block sits right after the tile words.
+static LookBack make_lb(const DevArrays &d)
 {
-    int blocks = std::max(1, div_up(c.N, kSweepTile));
-    LookBack lb = make_lb(d.tiles, d.tiles_cap, &d.sc->error);
-    k_sweep<<<blocks, kSweepThreads, 0, s>>>(c, d.state, d.infected, d.sc, lb, day);
+    LookBack lb;
+    lb.tiles = d.tiles;
+    lb.ctl = (int *)(d.tiles + d.tiles_cap);
+    lb.error = &d.sc->error;
+    return lb;
+}
+
+cudaError_t launch_sweep(const DevArrays &d, int day, cudaStream_t s)
+{
+    const int blocks = d.P / kSweepTile;
+    k_sweep<<<blocks, kSweepThreads, 0, s>>>(d.ic, d.is, d.tile_inst, d.K, d.state, d.infected, d.infected_inst, d.sc,
+                                             make_lb(d), day);
     count_launch();
     return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------ schedules
 // Weekday schedule (kernel_assignWeekdayAfterschoolAndErrands, PandemicSim.cu:2972-3022):
-// counter E0 + g -> persons 2g, 2g+1.  Hour-0 keys at [0,N), hour-1 keys at [N,2N).
-// Weekday destinations lie in [lo, L), lo = first location of type 8 (afterschool),
-// so the bucket index is hour * R + dest - lo with R = L - lo (order-preserving).
+// counter E0 + g -> the instance's persons 2g, 2g+1.  Hour-0 keys at [0,N), hour-1
+// keys at [N,2N) of the instance's key slots.  Weekday destinations lie in [lo, L),
+// lo = first location of type 8 (afterschool), so the instance's bucket is
+// hour * R + dest - lo with R = L - lo (order-preserving); the global bucket adds the
+// instance's weekday bucket base.
 __device__ __forceinline__ void weekday_pair_keys(const SimConst &c, const uint32_t w[4], int k, bool adult, int lo,
                                                   int R, int &k1, int &k2)
 {
@@ -889,35 +898,41 @@ __device__ __forceinline__ bool is_marked(const uint32_t *mark, int b) { return 
 // the same Threefry block, :3697-3702; children use the afterschool profile), and on
 // weekends the two errand slots picked by word 3 of the infection counter's block
 // (:1892, :1909, :1929).
-__global__ void k_mark_buckets(SimConst c, const uint8_t *age, const int32_t *infected, int weekend, uint32_t *mark,
-                               const Scalars *sc)
+__global__ void k_mark_buckets(const InstConst *ic, const InstState *is, const uint8_t *age, const int32_t *infected,
+                               const int32_t *infected_inst, int weekend, uint32_t *mark, const Scalars *sc)
 {
     if (sc->done) return;
-    const TfKey key = make_key(c);
     const int I = sc->infected;
-    const unsigned long long E0 = sc->errand_offset, R0 = sc->infect_offset;
     for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < I; pos += gridDim.x * blockDim.x) {
-        const int me = infected[pos];
+        const int k = infected_inst[pos];
+        const InstConst &ik = ic[k];
+        const SimConst &c = ik.c;
+        const InstState &s = is[k];
+        const TfKey key = make_key(c);
+        const int me = infected[pos] - ik.pbase;   // the instance's person number
+        const int lpos = pos - s.start;            // the instance's list position
         if (weekend) {
             const int lo = c.type_offset[9], R = c.L - lo;
             int d[3];
-            weekend_errands(c, key, E0 + 2ull * (unsigned long long)me, lo, R, d);
+            weekend_errands(c, key, s.errand_offset + 2ull * (unsigned long long)me, lo, R, d);
             uint32_t w[4];
-            tf2x64(key, R0 + 6ull * (unsigned long long)pos, w);
+            tf2x64(key, s.infect_offset + 6ull * (unsigned long long)lpos, w);
             const int prof = (int)(w[3] % 6u);
 #pragma unroll
-            for (int k = 0; k < 2; k++) {
-                const int b = d[c_weekend_assign[prof][k]];
+            for (int j = 0; j < 2; j++) {
+                const int b = ik.bbase[1] + d[c_weekend_assign[prof][j]];
                 atomicOr(&mark[b >> 5], 1u << (b & 31));
             }
         } else {
             const int lo = c.type_offset[8], R = c.L - lo;
             uint32_t w[4];
-            tf2x64(key, E0 + (uint64_t)(me / 2), w);
-            const bool adult = age[me] == 5;
+            tf2x64(key, s.errand_offset + (uint64_t)(me / 2), w);
+            const bool adult = age[infected[pos]] == 5;
             const int slot = 2 * (me & 1);
             int k1, k2;
             weekday_pair_keys(c, w, me & 1, adult, lo, R, k1, k2);
+            k1 += ik.bbase[0];
+            k2 += ik.bbase[0];
             const int prof = adult ? (int)((w[slot] ^ w[slot + 1]) % 3u) : 3;
             if (c_weekday_assign[prof][0] > 0) atomicOr(&mark[k1 >> 5], 1u << (k1 & 31));
             if (c_weekday_assign[prof][1] > 0) atomicOr(&mark[k2 >> 5], 1u << (k2 & 31));
@@ -925,41 +940,45 @@ __global__ void k_mark_buckets(SimConst c, const uint8_t *age, const int32_t *in
     }
 }
 
-// Schedule kernel, one tile of 4096 persons per block.  Warps own 512 consecutive
-// persons and walk them in rounds (weekday: 64 persons a round, a pair per lane, one
-// Threefry block per pair; weekend: 32 persons a round, one per lane), so key writes
-// are coalesced.  The kernel writes every person's keys, counts the entries of
-// marked buckets and appends those entries as (key, person) in ascending person
-// order (warp scans + block scan + decoupled look-back): the order the radix sort
-// needs for stability.  Per-round marked counts of a lane are packed in one register
-// between the two phases.
-constexpr int kSchedThreads = 256, kSchedTile = 4096, kSchedWarpPersons = 512;
-
-__device__ __forceinline__ int warp_inclusive_scan(int v)
-{
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += y;
-    }
-    return v;
-}
+// Schedule kernel, one person tile per block.  Warps own 512 consecutive persons and
+// walk them in rounds (weekday: 64 persons a round, a pair per lane, one Threefry
+// block per pair; weekend: 32 persons a round, one per lane), so key writes are
+// coalesced.  The kernel writes every person's keys, counts the entries of marked
+// buckets and appends those entries as (key, person) in ascending person order
+// (warp scans + block scan + decoupled look-back): the order the radix sort needs
+// for stability.  Per-round marked counts of a lane are packed in one register
+// between the two phases.  The instance's constants are staged in shared memory.
+constexpr int kSchedThreads = 256, kSchedTile = kPersonTile, kSchedWarpPersons = 512;
 
 template <bool WEEKEND>
-__global__ void __launch_bounds__(kSchedThreads) k_sched(SimConst c, const uint8_t *age, const uint32_t *mark,
-                                                         int32_t *keys, int32_t *count, uint32_t *ckeys,
-                                                         uint32_t *cvals, Scalars *sc, LookBack lb)
+__global__ void __launch_bounds__(kSchedThreads) k_sched(const InstConst *ic, const InstState *is,
+                                                         const int32_t *tile_inst, const uint8_t *age,
+                                                         const uint32_t *mark, int32_t *keys, int32_t *count,
+                                                         uint32_t *ckeys, uint32_t *cvals, Scalars *sc, LookBack lb,
+                                                         int day)
 {
     if (*(volatile int *)&sc->done) return;
     int tile;
     unsigned epoch;
     lookback_begin(lb, tile, epoch);
+    const int inst = tile_inst[tile];
+    __shared__ SimConst s_c;
+    {
+        const int *src = reinterpret_cast<const int *>(&ic[inst].c);
+        int *dst = reinterpret_cast<int *>(&s_c);
+        for (int i = threadIdx.x; i < (int)(sizeof(SimConst) / 4); i += kSchedThreads) dst[i] = src[i];
+    }
+    __syncthreads();
+    const SimConst &c = s_c;
     const TfKey key = make_key(c);
-    const unsigned long long E0 = sc->errand_offset;
-    const int N = c.N;
+    const int pbase = ic[inst].pbase;
+    const int bb = ic[inst].bbase[WEEKEND ? 1 : 0];
+    int32_t *kk = keys + ic[inst].kbase;                                   // the instance's key slots
+    const int NK = c.N;                                                    // key layout
+    const int N = instance_running(ic[inst], is[inst], day) ? c.N : 0;    // persons to schedule
+    const unsigned long long E0 = is[inst].errand_offset;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int wbase = tile * kSchedTile + warp * kSchedWarpPersons;
+    const int wbase = tile * kSchedTile - pbase + warp * kSchedWarpPersons;  // the instance's person number
     constexpr int kRounds = WEEKEND ? 16 : 8;
     constexpr int kBits = WEEKEND ? 2 : 3;  // marked entries per lane and round: <= 3 / <= 4
     uint32_t cpack = 0;
@@ -976,9 +995,10 @@ __global__ void __launch_bounds__(kSchedThreads) k_sched(SimConst c, const uint8
                 weekend_errands(c, key, E0 + 2ull * (unsigned long long)p, lo, R, d);
 #pragma unroll
                 for (int k = 0; k < 3; k++) {
-                    keys[3 * (size_t)p + k] = d[k];
-                    if (is_marked(mark, d[k])) {
-                        atomicAdd(&count[d[k]], 1);
+                    const int b = bb + d[k];
+                    kk[3 * (size_t)p + k] = b;
+                    if (is_marked(mark, b)) {
+                        atomicAdd(&count[b], 1);
                         cnt++;
                     }
                 }
@@ -1000,9 +1020,11 @@ __global__ void __launch_bounds__(kSchedThreads) k_sched(SimConst c, const uint8
                     const int q = p + k;
                     if (q < N) {
                         int k1, k2;
-                        weekday_pair_keys(c, w, k, age[q] == 5, lo, R, k1, k2);
-                        keys[q] = k1;
-                        keys[(size_t)N + q] = k2;
+                        weekday_pair_keys(c, w, k, age[pbase + q] == 5, lo, R, k1, k2);
+                        k1 += bb;
+                        k2 += bb;
+                        kk[q] = k1;
+                        kk[(size_t)NK + q] = k2;
                         if (is_marked(mark, k1)) {
                             atomicAdd(&count[k1], 1);
                             cnt++;
@@ -1054,10 +1076,10 @@ __global__ void __launch_bounds__(kSchedThreads) k_sched(SimConst c, const uint8
                 const int p = wbase + 32 * j + lane;
 #pragma unroll
                 for (int k = 0; k < 3; k++) {
-                    const int b = keys[3 * (size_t)p + k];
+                    const int b = kk[3 * (size_t)p + k];
                     if (is_marked(mark, b)) {
                         ckeys[pos] = (uint32_t)b;
-                        cvals[pos] = (uint32_t)p;
+                        cvals[pos] = (uint32_t)(pbase + p);
                         pos++;
                     }
                 }
@@ -1069,10 +1091,10 @@ __global__ void __launch_bounds__(kSchedThreads) k_sched(SimConst c, const uint8
                     if (q < N) {
 #pragma unroll
                         for (int h = 0; h < 2; h++) {
-                            const int b = keys[(size_t)h * N + q];
+                            const int b = kk[(size_t)h * NK + q];
                             if (is_marked(mark, b)) {
                                 ckeys[pos] = (uint32_t)b;
-                                cvals[pos] = (uint32_t)q;
+                                cvals[pos] = (uint32_t)(pbase + q);
                                 pos++;
                             }
                         }
@@ -1091,37 +1113,40 @@ int day_buckets(const SimConst &c, bool weekend)
 }
 
 // mark (or mark everything for complete tables), then the schedule kernel
-cudaError_t launch_schedule(const SimConst &c, const DevArrays &d, bool weekend, bool full_tables, cudaStream_t s)
+cudaError_t launch_schedule(const DevArrays &d, bool weekend, int day, bool full_tables, cudaStream_t s)
 {
-    const int B = day_buckets(c, weekend);
+    const int B = d.buckets[weekend ? 1 : 0];
     cudaError_t e = cudaMemsetAsync(d.mark, full_tables ? 0xFF : 0, ((size_t)B / 32 + 1) * 4, s);
     if (e != cudaSuccess) return e;
     if (!full_tables) {
-        k_mark_buckets<<<sm_count() * 4, 128, 0, s>>>(c, d.age, d.infected, weekend ? 1 : 0, d.mark, d.sc);
+        k_mark_buckets<<<sm_count() * 4, 128, 0, s>>>(d.ic, d.is, d.age, d.infected, d.infected_inst, weekend ? 1 : 0,
+                                                      d.mark, d.sc);
         count_launch();
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    const int blocks = std::max(1, div_up(c.N, kSchedTile));
-    LookBack lb = make_lb(d.tiles, d.tiles_cap, &d.sc->error);
+    const int blocks = d.P / kSchedTile;
+    const LookBack lb = make_lb(d);
     if (weekend)
-        k_sched<true><<<blocks, kSchedThreads, 0, s>>>(c, d.age, d.mark, d.keys, d.bkt_count, d.rk1, d.rv1, d.sc, lb);
+        k_sched<true><<<blocks, kSchedThreads, 0, s>>>(d.ic, d.is, d.tile_inst, d.age, d.mark, d.keys, d.bkt_count,
+                                                       d.rk1, d.rv1, d.sc, lb, day);
     else
-        k_sched<false><<<blocks, kSchedThreads, 0, s>>>(c, d.age, d.mark, d.keys, d.bkt_count, d.rk1, d.rv1, d.sc, lb);
+        k_sched<false><<<blocks, kSchedThreads, 0, s>>>(d.ic, d.is, d.tile_inst, d.age, d.mark, d.keys, d.bkt_count,
+                                                        d.rk1, d.rv1, d.sc, lb, day);
     count_launch();
     return cudaGetLastError();
 }
 
 // The day's radix sort starts from the marked entries the schedule appended to
 // (rk1, rv1), in person order; their count is on the device.
-static RadixArgs day_radix_args(const SimConst &c, const DevArrays &d, bool weekend)
+static RadixArgs day_radix_args(const DevArrays &d, bool weekend)
 {
     RadixArgs r;
     r.keys = d.rk1;
     r.vals = d.rv1;
-    r.E = (weekend ? 3 : 2) * c.N;
-    r.buckets = day_buckets(c, weekend);
-    r.N = c.N;
+    r.E = (weekend ? 3 : 2) * d.P;
+    r.buckets = d.buckets[weekend ? 1 : 0];
+    r.N = d.P;
     r.person_mode = weekend ? 2 : 1;
     r.count_dev = &d.sc->marked_entries;
     r.k0 = d.rk0; r.v0 = d.rv0; r.k1 = d.rk1; r.v1 = d.rv1;
@@ -1134,9 +1159,9 @@ static RadixArgs day_radix_args(const SimConst &c, const DevArrays &d, bool week
     return r;
 }
 
-cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s)
+cudaError_t launch_bucket_scan(const DevArrays &d, bool weekend, cudaStream_t s)
 {
-    const int B = day_buckets(c, weekend);
+    const int B = d.buckets[weekend ? 1 : 0];
     const int P = radix_passes(B);
     cudaError_t e = launch_scan_exclusive(d.bkt_count, d.bkt_offset, B, 1, d.tiles, (int *)(d.tiles + d.tiles_cap),
                                           &d.sc->error, &d.sc->done, P, d.digit_hist, s, nullptr, nullptr,
@@ -1147,9 +1172,9 @@ cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weeke
     return cudaGetLastError();
 }
 
-cudaError_t launch_bucket_sort(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s)
+cudaError_t launch_bucket_sort(const DevArrays &d, bool weekend, cudaStream_t s)
 {
-    return launch_radix_sort(day_radix_args(c, d, weekend), s);
+    return launch_radix_sort(day_radix_args(d, weekend), s);
 }
 
 // ------------------------------------------------------------------ infection
@@ -1173,7 +1198,7 @@ __device__ __forceinline__ int select_victim(int self, int off, int count, uint3
 }
 
 struct Infector {
-    int me, pos;
+    int me, pos;   // global person id, position in the batch's infected list
     float prob[2];
     int gen[2];
 };
@@ -1181,6 +1206,8 @@ struct Infector {
 // device_processContacts (PandemicSim.cu:3106-3233) with the claim rule: a
 // successful draw on a victim whose strain status was susceptible at the start of
 // the day claims (victim, strain) with key (position, slot); the smallest key wins.
+// A victim is only ever drawn by infectors of its own instance, whose list positions
+// keep the instance's order.
 template <int NC>
 __device__ __forceinline__ void process_contacts(const SimConst &c, const TfKey &key, const Infector &inf,
                                                  unsigned long long ctr, const int (&victims)[NC],
@@ -1236,30 +1263,35 @@ __device__ __forceinline__ void infector_state(const SimConst &c, Infector &inf,
 }
 
 struct InfectArgs {
+    const InstConst *ic;
+    const InstState *is;
     const uint32_t *state;
     const uint8_t *gen_p, *gen_s, *age;
     const int32_t *household, *hh_offset, *workplace, *wp_people, *wp_offset;
-    const int32_t *keys, *bkt_offset, *bkt_people, *infected;
+    const int32_t *keys, *bkt_offset, *bkt_people, *infected, *infected_inst;
     unsigned long long *claim;
     int32_t *new_list;
     Scalars *sc;
 };
 
 // kernel_doWeekday + device_makeContacts_weekday (PandemicSim.cu:3236-3308, :1669-1829)
-__global__ void __launch_bounds__(128) k_infect_weekday(SimConst c, InfectArgs a, int day)
+__global__ void __launch_bounds__(128) k_infect_weekday(InfectArgs a, int day)
 {
     Scalars *sc = a.sc;
     if (sc->done) return;
-    const TfKey key = make_key(c);
     const int I = sc->infected;
-    const unsigned long long R0 = sc->infect_offset, E0 = sc->errand_offset;
-    const int N = c.N;
     for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < I; pos += gridDim.x * blockDim.x) {
+        const int inst = a.infected_inst[pos];
+        const InstConst &ik = a.ic[inst];
+        const SimConst &c = ik.c;
+        const InstState &s = a.is[inst];
+        const TfKey key = make_key(c);
         Infector inf;
         inf.pos = pos;
         inf.me = a.infected[pos];
         const int me = inf.me;
-        const unsigned long long ctr = R0 + 6ull * (unsigned long long)pos;
+        const int lme = me - ik.pbase;  // the instance's person number
+        const unsigned long long ctr = s.infect_offset + 6ull * (unsigned long long)(pos - s.start);
         uint32_t w[8];
         tf2x64(key, ctr, w);
         tf2x64(key, ctr + 1, w + 4);
@@ -1278,15 +1310,16 @@ __global__ void __launch_bounds__(128) k_infect_weekday(SimConst c, InfectArgs a
         // workplace or school: max-contacts of its type
         const int wp = a.workplace[me];
         const int woff = a.wp_offset[wp], wcnt = a.wp_offset[wp + 1] - woff;
-        const int desired = workplace_max_contacts(c, wp);
+        const int desired = workplace_max_contacts(c, wp - ik.lbase);
         // errands / afterschool: destinations from today's keys; the adult
         // profile is regenerated from the schedule counter (:3667-3705)
-        const int dest[2] = {a.keys[me], a.keys[N + me]};
+        const int32_t *kk = a.keys + ik.kbase;
+        const int dest[2] = {kk[lme], kk[c.N + lme]};
         int prof = 3;
         if (adult) {
             uint32_t e[4];
-            tf2x64(key, E0 + (uint64_t)(me / 2), e);
-            const int slot = 2 * (me % 2);
+            tf2x64(key, s.errand_offset + (uint64_t)(lme / 2), e);
+            const int slot = 2 * (lme % 2);
             prof = (int)((e[slot] ^ e[slot + 1]) % 3u);
         }
         int made = 3;
@@ -1323,19 +1356,23 @@ __global__ void __launch_bounds__(128) k_infect_weekday(SimConst c, InfectArgs a
 }
 
 // kernel_doWeekend + device_makeContacts_weekend (PandemicSim.cu:3311-3379, :1833-1950)
-__global__ void __launch_bounds__(128) k_infect_weekend(SimConst c, InfectArgs a, int day)
+__global__ void __launch_bounds__(128) k_infect_weekend(InfectArgs a, int day)
 {
     Scalars *sc = a.sc;
     if (sc->done) return;
-    const TfKey key = make_key(c);
     const int I = sc->infected;
-    const unsigned long long R0 = sc->infect_offset;
     for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < I; pos += gridDim.x * blockDim.x) {
+        const int inst = a.infected_inst[pos];
+        const InstConst &ik = a.ic[inst];
+        const SimConst &c = ik.c;
+        const InstState &s = a.is[inst];
+        const TfKey key = make_key(c);
         Infector inf;
         inf.pos = pos;
         inf.me = a.infected[pos];
         const int me = inf.me;
-        const unsigned long long ctr = R0 + 6ull * (unsigned long long)pos;
+        const int lme = me - ik.pbase;
+        const unsigned long long ctr = s.infect_offset + 6ull * (unsigned long long)(pos - s.start);
         uint32_t w[4];
         tf2x64(key, ctr, w);
         int victims[5], kv[5];
@@ -1351,7 +1388,7 @@ __global__ void __launch_bounds__(128) k_infect_weekend(SimConst c, InfectArgs a
         // Threefry-2x32 on the low seed words with counter (u32)(ctr + 1) (:1895-1901)
         uint32_t v2[2];
         tf2x32(key, (uint32_t)(ctr + 1), v2);
-        const int32_t *k3 = a.keys + 3 * (size_t)me;
+        const int32_t *k3 = a.keys + ik.kbase + 3 * (size_t)lme;
 #pragma unroll
         for (int j = 0; j < 2; j++) {
             const int loc = k3[c_weekend_assign[prof][j]];
@@ -1364,17 +1401,19 @@ __global__ void __launch_bounds__(128) k_infect_weekend(SimConst c, InfectArgs a
     }
 }
 
-cudaError_t launch_infect(const SimConst &c, const DevArrays &d, bool weekend, int day, cudaStream_t s)
+cudaError_t launch_infect(const DevArrays &d, bool weekend, int day, cudaStream_t s)
 {
     InfectArgs a;
+    a.ic = d.ic; a.is = d.is;
     a.state = d.state; a.gen_p = d.gen_p; a.gen_s = d.gen_s; a.age = d.age;
     a.household = d.household; a.hh_offset = d.hh_offset; a.workplace = d.workplace;
     a.wp_people = d.wp_people; a.wp_offset = d.wp_offset; a.keys = d.keys;
     a.bkt_offset = d.bkt_offset; a.bkt_people = d.bkt_people; a.infected = d.infected;
+    a.infected_inst = d.infected_inst;
     a.claim = d.claim; a.new_list = d.new_list; a.sc = d.sc;
     int blocks = sm_count() * 16;
-    if (weekend) k_infect_weekend<<<blocks, 128, 0, s>>>(c, a, day);
-    else k_infect_weekday<<<blocks, 128, 0, s>>>(c, a, day);
+    if (weekend) k_infect_weekend<<<blocks, 128, 0, s>>>(a, day);
+    else k_infect_weekday<<<blocks, 128, 0, s>>>(a, day);
     count_launch();
     return cudaGetLastError();
 }
@@ -1415,26 +1454,31 @@ cudaError_t launch_apply(const DevArrays &d, int day, cudaStream_t s)
 }
 
 // ================================================================== final
-__global__ void k_gen_hist(const uint8_t *gen_p, const uint8_t *gen_s, int N, int *hist)
+// final_countReproduction's generation counts (PandemicSim.cu:2227-2304) for every
+// instance: one block per person tile, histogram in shared memory.
+__global__ void k_gen_hist(const InstConst *ic, const int32_t *tile_inst, const uint8_t *gen_p, const uint8_t *gen_s,
+                           int *hist)
 {
     __shared__ int h[512];
     for (int i = threadIdx.x; i < 512; i += blockDim.x) h[i] = 0;
     __syncthreads();
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const int k = tile_inst[blockIdx.x];
+    const long long first = (long long)blockIdx.x * kPersonTile;
+    const long long end = (long long)ic[k].pbase + ic[k].c.N;
+    for (long long i = first + threadIdx.x; i < first + kPersonTile && i < end; i += blockDim.x) {
         atomicAdd(&h[gen_p[i]], 1);
         atomicAdd(&h[256 + gen_s[i]], 1);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < 512; i += blockDim.x)
-        if (h[i]) atomicAdd(&hist[i], h[i]);
+        if (h[i]) atomicAdd(&hist[(size_t)k * 512 + i], h[i]);
 }
 
-cudaError_t launch_gen_hist(const uint8_t *gen_p, const uint8_t *gen_s, int N, int *hist512, cudaStream_t s)
+cudaError_t launch_gen_hist(const DevArrays &d, int *hist, cudaStream_t s)
 {
-    cudaError_t e = cudaMemsetAsync(hist512, 0, 512 * sizeof(int), s);
+    cudaError_t e = cudaMemsetAsync(hist, 0, (size_t)d.K * 512 * sizeof(int), s);
     if (e != cudaSuccess) return e;
-    int blocks = std::max(1, std::min(div_up(N, 256), sm_count() * 4));
-    k_gen_hist<<<blocks, 256, 0, s>>>(gen_p, gen_s, N, hist512);
+    k_gen_hist<<<d.P / kPersonTile, 256, 0, s>>>(d.ic, d.tile_inst, d.gen_p, d.gen_s, hist);
     count_launch();
     return cudaGetLastError();
 }

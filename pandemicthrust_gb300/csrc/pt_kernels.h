@@ -10,8 +10,10 @@ namespace ptk {
 constexpr int kTypes = 14;
 constexpr int kMaxDays = 256;
 
-// Per-simulation constants, passed by value to every kernel (kernel-parameter
-// space is a uniform constant bank).
+constexpr int kPersonTile = 4096;  // persons per sweep / schedule tile
+
+// Constants of one simulation (setup kernels take them by value; the day kernels
+// read them from the InstConst array).
 struct SimConst {
     int N, H, L;
     int type_count[kTypes];
@@ -23,55 +25,85 @@ struct SimConst {
     uint64_t workplace_offset;     // W0: counter base of the workplace draws
 };
 
-// Device-resident scalars of one simulation.  The day loop reads and updates
-// these on the device, so a whole run needs no host round trip.
-struct Scalars {
+// One simulation of a batch and where its rows sit in the batch-wide arrays.  Every
+// instance's persons start on a person-tile boundary, so a sweep or schedule tile
+// belongs to exactly one instance; the persons up to the next boundary are padding
+// (never infected, never counted, in no table).
+struct InstConst {
+    SimConst c;            // c.N = the instance's persons
+    int pbase;             // first global person (a multiple of kPersonTile)
+    int hbase;             // first global household slot; H + 1 slots, the last one
+                           // holds the padding persons
+    int lbase;             // first global location
+    int bbase[2];          // first global bucket of the weekday / weekend errand tables
+    int max_days;
+    long long kbase;       // first schedule-key slot (3 * pbase)
+};
+
+// Device-resident state of one simulation.  The day loop reads and updates it on
+// the device, so a whole run needs no host round trip.
+struct InstState {
     unsigned long long rand_offset;     // next free Random123 counter
-    unsigned long long materialised_sum;  // schedule entries written to bucket tables, all days
     unsigned long long errand_offset;   // E0 of the current day's schedule
     unsigned long long infect_offset;   // R0 of the current day's contacts
     int infected;                       // infected count of the current day
+    int start;                          // their first position in the batch's infected list
     int done;                           // set once a day counts zero infected
     int days_run;                       // statistics rows written
-    int day;                            // current day index
-    int new_count;                      // entries in the new-infection list
-    int tile_ticket;                    // dynamic tile index of look-back kernels
-    int tile_ticket2;
-    int error;                          // nonzero: a bounded device wait gave up
-    int error_site;
-    int marked_entries;                 // schedule entries in today's materialised buckets
-    int unused;
-    int adults;
-    int pad[2];
+    int day;                            // last day run
+    int tile_infected;                  // infected counted so far by today's sweep tiles
     int counts[kMaxDays][16];           // per-day status bins
     int infected_per_day[kMaxDays];
 };
 
-// Device pointers of one simulation (all owned by one arena allocation).
+// Batch-wide device scalars.
+struct Scalars {
+    unsigned long long materialised_sum;  // schedule entries written to bucket tables, all days
+    int infected;                         // length of today's infected list (all instances)
+    int done;                             // set once a day finds no instance with infected
+    int day;                              // current day index
+    int new_count;                        // entries in the new-infection list
+    int error;                            // nonzero: a bounded device wait gave up
+    int error_site;
+    int marked_entries;                   // schedule entries in today's materialised buckets
+    int pad;
+};
+
+// Device pointers of a batch of simulations (one simulation is a batch of one).
+// Person, household, location and bucket ids are global: an instance's ids are its
+// local ids plus its bases.
 struct DevArrays {
-    uint32_t *state;          // N: status_p | status_s<<8 | day_p<<16 | day_s<<24
-    uint8_t *gen_p, *gen_s;   // N
-    uint8_t *age;             // N
-    int32_t *household;       // N
-    int32_t *hh_offset;       // H+1
-    int32_t *workplace;       // N
-    int32_t *wp_people;       // N
-    int32_t *wp_offset;       // L+1
-    int32_t *keys;            // 3N schedule keys (compact bucket indices)
-    int32_t *bkt_offset;      // buckets+1 (at most 10L+1)
+    uint32_t *state;          // P: status_p | status_s<<8 | day_p<<16 | day_s<<24
+    uint8_t *gen_p, *gen_s;   // P
+    uint8_t *age;             // P
+    int32_t *household;       // P
+    int32_t *hh_offset;       // household slots + 1
+    int32_t *workplace;       // P
+    int32_t *wp_people;       // P (padding persons last, in the spare bucket)
+    int32_t *wp_offset;       // locations + 2
+    int32_t *keys;            // 3P schedule keys (global bucket indices)
+    int32_t *bkt_offset;      // buckets+1
     int32_t *bkt_count;       // buckets histogram, zero between uses
-    int32_t *bkt_people;      // 3N person ids bucket by bucket, ascending in each
-    uint32_t *rk0, *rv0, *rk1, *rv1;  // 3N each: radix ping-pong keys/values
-    unsigned long long *radix_status;  // ceil(3N/4096) x 256 epoch-tagged look-back words
+    int32_t *bkt_people;      // 3P person ids bucket by bucket, ascending in each
+    uint32_t *rk0, *rv0, *rk1, *rv1;  // 3P each: radix ping-pong keys/values
+    unsigned long long *radix_status;  // ceil(3P/4096) x 256 epoch-tagged look-back words
     int *radix_ctl;           // ticket, finished
     int *digit_hist;          // 4 x 256
     int *digit_base;          // 4 x 256
     uint32_t *mark;           // bitmap over today's buckets: 1 = materialise
-    int32_t *infected;        // N ascending infected ids
-    unsigned long long *claim;// 2N (victim, strain) -> min attempt key
-    int32_t *new_list;        // 2N first claims of the day
+    int32_t *infected;        // P ascending infected ids
+    int32_t *infected_inst;   // P: instance of each infected list position
+    unsigned long long *claim;// 2P (victim, strain) -> min attempt key
+    int32_t *new_list;        // 2P first claims of the day
     unsigned long long *tiles;// look-back tile status words
     int tiles_cap;
+    const InstConst *ic;      // K
+    InstState *is;            // K
+    const int32_t *tile_inst; // P / kPersonTile: instance of each person tile
+    int K;
+    int P;                    // persons including padding, a multiple of kPersonTile
+    int buckets[2];           // weekday / weekend buckets over all instances
+    int locations;            // locations over all instances
     Scalars *sc;
 };
 
@@ -80,15 +112,19 @@ int sm_count();
 
 // ---- setup
 cudaError_t launch_household_types(const SimConst &c, uint8_t *types, int32_t *sizes, int *adults,
-                                   cudaStream_t s);
+                                   int *persons, cudaStream_t s);
 cudaError_t launch_scan_exclusive(const int32_t *in, int32_t *out, int n, int clear_in,
                                   unsigned long long *tiles, int *ctl, int *error,
                                   const int *skip, int passes, int *digit_hist, cudaStream_t s,
                                   const uint32_t *mark = nullptr, int *total_out = nullptr,
                                   unsigned long long *total_accum = nullptr);
-cudaError_t launch_generate_households(const SimConst &c, const uint8_t *types, const int32_t *hh_offset,
+cudaError_t launch_generate_households(const uint8_t *types, const int32_t *hh_offset, int slots,
                                        int32_t *household, uint8_t *age, cudaStream_t s);
-cudaError_t launch_assign_workplaces(const SimConst &c, uint8_t *age, int32_t *workplace, cudaStream_t s);
+cudaError_t launch_assign_workplaces(const SimConst &c, uint8_t *age, int32_t *workplace, int loc_base,
+                                     cudaStream_t s);
+// household slots of the padding persons, and the padding persons themselves
+cudaError_t launch_batch_padding(const DevArrays &d, uint8_t *types, int32_t *sizes, int spare_location,
+                                 bool persons, cudaStream_t s);
 cudaError_t launch_count_keys(const int32_t *keys, int n, int32_t *count, cudaStream_t s);
 
 // Stable LSD radix sort of E keys in [0, buckets) with implicit person values
@@ -113,20 +149,24 @@ cudaError_t launch_bucket_table(const RadixArgs &r, int32_t *counts, bool count_
                                 unsigned long long *tiles, int *lb_ctl, int *digit_hist, cudaStream_t s);
 cudaError_t launch_init_status(int N, uint32_t *state, uint8_t *gen_p, uint8_t *gen_s,
                                unsigned long long *claim, cudaStream_t s);
+// every instance's device state back to "set up, day 0": rand_offset after setup is
+// H/4 (household types) + N/4 (workplaces)
+cudaError_t launch_reset_instances(const DevArrays &d, cudaStream_t s);
 cudaError_t launch_seed_infected(const int32_t *seeds, int P, int S, uint32_t *state, uint8_t *gen_p,
                                  uint8_t *gen_s, cudaStream_t s);
 
-// ---- day
-cudaError_t launch_sweep(const SimConst &c, const DevArrays &d, int day, cudaStream_t s);
-cudaError_t launch_schedule(const SimConst &c, const DevArrays &d, bool weekend, bool full_tables, cudaStream_t s);
-int day_buckets(const SimConst &c, bool weekend);
-cudaError_t launch_bucket_scan(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
-cudaError_t launch_bucket_sort(const SimConst &c, const DevArrays &d, bool weekend, cudaStream_t s);
-cudaError_t launch_infect(const SimConst &c, const DevArrays &d, bool weekend, int day, cudaStream_t s);
+// ---- day (every instance of the batch in each launch)
+cudaError_t launch_sweep(const DevArrays &d, int day, cudaStream_t s);
+cudaError_t launch_schedule(const DevArrays &d, bool weekend, int day, bool full_tables, cudaStream_t s);
+cudaError_t launch_bucket_scan(const DevArrays &d, bool weekend, cudaStream_t s);
+cudaError_t launch_bucket_sort(const DevArrays &d, bool weekend, cudaStream_t s);
+cudaError_t launch_infect(const DevArrays &d, bool weekend, int day, cudaStream_t s);
 cudaError_t launch_apply(const DevArrays &d, int day, cudaStream_t s);
+// weekday / weekend buckets of one instance (compact keys hour * R + dest - lo)
+int day_buckets(const SimConst &c, bool weekend);
 
-// ---- final
-cudaError_t launch_gen_hist(const uint8_t *gen_p, const uint8_t *gen_s, int N, int *hist512, cudaStream_t s);
+// ---- final: per-instance generation histograms, K x 512 (pandemic 0..255, seasonal 256..511)
+cudaError_t launch_gen_hist(const DevArrays &d, int *hist, cudaStream_t s);
 
 uint64_t launches();
 void add_launches(int64_t n);  // kernels run by a replayed graph

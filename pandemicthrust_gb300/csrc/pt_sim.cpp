@@ -1,9 +1,14 @@
 // pt_sim.cpp - C ABI of the simulation: lifecycle, the PandemicSim host flow
 // (setupSim / runToCompletion / doWeekday|doWeekend / final_countReproduction) and
-// device-memory ownership.  All device memory of a simulation lives in one arena.
+// device-memory ownership, for one simulation (pt_sim) and for a batch of
+// independent simulations (pt_batch).  Both are an Engine: K instances whose persons,
+// households, locations and buckets share batch-wide arrays, each instance in its own
+// range.  A pt_sim is an Engine with one instance.  All device memory of an engine
+// lives in two allocations (a small one and an arena).
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -33,30 +38,48 @@ size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 thread_local std::string g_create_error;
 
-}  // namespace
-
-struct pt_sim {
+// One simulation of an engine: its inputs and the host mirror of its results.
+struct Instance {
     pt_params params;
     int core_seed = 0;
     pth::Derived derived;
     std::unique_ptr<pth::GlibcRand> rng;
-    std::vector<int32_t> seed_list;
+    std::vector<int32_t> seed_list;   // the instance's person numbers
     ptk::SimConst c;
+    int adults = 0;
+    int day = 0;                      // next day to run
+    bool stopped = false;             // a day counted zero infected
+    int days_run = 0;
+    std::vector<int> counts;          // kMaxDays * 16
+    std::vector<int> infected;        // kMaxDays
+    float max_prop = 0.f;
+    int max_prop_day = 0;
+};
+
+// Stage boundaries recorded per day when timing is on.
+enum { kStSweep, kStSchedule, kStScan, kStRadix, kStInfect, kStApply, kStages };
+
+}  // namespace
+
+struct Engine {
+    std::vector<Instance> inst;
+    std::vector<ptk::InstConst> ic;   // host copy of the device array
     ptk::DevArrays d;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    char *setup_mem = nullptr;      // household types/sizes during setup
-    char *small_mem = nullptr;      // scalars, look-back words, histogram, household offsets
+    char *setup_mem = nullptr;        // household types/sizes during setup
+    char *small_mem = nullptr;        // scalars, instance records, look-back words, histograms, household offsets
     size_t small_bytes = 0;
     char *arena_mem = nullptr;
     size_t arena_bytes = 0;
     int32_t *d_seeds = nullptr;
-    int *d_hist = nullptr;
-    int adults = 0;
+    int seeds_p = 0, seeds_s = 0;     // pandemic / seasonal seeds over all instances
+    std::vector<int32_t> seed_global; // global person ids: all pandemic seeds, then all seasonal ones
+    int *d_hist = nullptr;            // K x 512
+    int64_t persons = 0;              // real persons over all instances
     bool setup_done = false;
-    int day = 0;                    // next day to run
-    bool stopped = false;           // a day counted zero infected
-    int days_run = 0;
+    int next_day = 0;                 // next global day to run
+    int max_days = 0;                 // longest max_days of the instances
     std::string err;
     bool timing = false;
     bool full_tables = false;             // materialise every bucket (tables complete for inspection)
@@ -64,44 +87,44 @@ struct pt_sim {
     std::vector<int> timed_days;
     float stage_ms[16] = {0};             // [weekday stages 0..7, weekend stages 8..15]
     int stage_days[2] = {0, 0};
-    // per-day results mirrored on the host
-    std::vector<int> counts;        // kMaxDays * 16
-    std::vector<int> infected;      // kMaxDays
-    float max_prop = 0.f;
-    int max_prop_day = 0;
     mutable uint64_t h2d_bytes = 0, d2h_bytes = 0;  // host<->device copies issued
-    // The whole day loop (days 0..max_days-1) captured once and replayed by pt_run.
-    // Every per-day decision (early stop, counters, offsets) reads device scalars,
-    // so the same graph serves every run after pt_reset_epidemic.
+    // The whole day loop (days 0..max_days-1) captured once and replayed by run().
+    // Every per-day decision (early stop, counters, offsets) reads device state, so
+    // the same graph serves every run after a reset.
     cudaGraphExec_t run_graph = nullptr;
     uint64_t graph_kernels = 0;
+
+    int K() const { return (int)inst.size(); }
+    ~Engine();
 };
+
+struct pt_sim : Engine {};
+struct pt_batch : Engine {};
 
 // Every host<->device copy of the library goes through these, so the bytes a call
 // moves across PCIe/C2C can be reported (pt_transfer_bytes).
-static cudaError_t pt_memcpy(const pt_sim *s, void *dst, const void *src, size_t n, cudaMemcpyKind k,
-                             cudaStream_t st)
+static cudaError_t pt_memcpy(const Engine *s, void *dst, const void *src, size_t n, cudaMemcpyKind k, cudaStream_t st)
 {
     if (k == cudaMemcpyHostToDevice) s->h2d_bytes += n;
     else if (k == cudaMemcpyDeviceToHost) s->d2h_bytes += n;
     return cudaMemcpyAsync(dst, src, n, k, st);
 }
 
-static cudaError_t pt_memcpy_sync(const pt_sim *s, void *dst, const void *src, size_t n, cudaMemcpyKind k)
+static cudaError_t pt_memcpy_sync(const Engine *s, void *dst, const void *src, size_t n, cudaMemcpyKind k)
 {
     cudaError_t e = pt_memcpy(s, dst, src, n, k, s->stream);
     if (e != cudaSuccess) return e;
     return cudaStreamSynchronize(s->stream);
 }
 
-static pt_status fail(pt_sim *s, pt_status st, const std::string &msg)
+static pt_status fail(Engine *s, pt_status st, const std::string &msg)
 {
     if (s) s->err = msg;
     else g_create_error = msg;
     return st;
 }
 
-static pt_status cuda_fail(pt_sim *s, cudaError_t e, const char *where)
+static pt_status cuda_fail(Engine *s, cudaError_t e, const char *where)
 {
     std::string m = std::string(where) + ": " + cudaGetErrorString(e);
     return fail(s, e == cudaErrorMemoryAllocation ? PT_ERR_OOM : PT_ERR_CUDA, m);
@@ -113,143 +136,197 @@ static pt_status cuda_fail(pt_sim *s, cudaError_t e, const char *where)
         if (_e != cudaSuccess) return cuda_fail(s, _e, where); \
     } while (0)
 
-extern "C" {
-
-pt_status pt_create(const pt_params *params, int core_seed, void *cuda_stream, pt_sim **out)
+Engine::~Engine()
 {
-    if (!params || !out) return fail(nullptr, PT_ERR_ARG, "null argument");
-    *out = nullptr;
-    std::unique_ptr<pt_sim> s(new pt_sim());
-    s->params = *params;
-    s->core_seed = core_seed;
-    s->rng.reset(new pth::GlibcRand((unsigned int)core_seed));
-    const char *why = nullptr;
-    pt_status st = pth::derive(*params, core_seed, s->derived, *s->rng, &why);
-    if (st != PT_OK) return fail(nullptr, st, why ? why : "invalid parameters");
-    ptk::SimConst &c = s->c;
-    std::memset(&c, 0, sizeof(c));
-    c.H = s->derived.households;
-    c.L = s->derived.workplaces;
-    for (int t = 0; t < 14; t++) {
-        c.type_count[t] = s->derived.type_count[t];
-        c.type_offset[t] = s->derived.type_offset[t];
+    if (stream) cudaStreamSynchronize(stream);
+    if (run_graph) cudaGraphExecDestroy(run_graph);
+    cudaFree(arena_mem);
+    cudaFree(setup_mem);
+    cudaFree(small_mem);
+    for (auto &e : day_events)
+        if (e) cudaEventDestroy(e);
+    if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+// PandemicSim::PandemicSim() for each instance: seeds, scaling, infection data.
+// Needs no device: parameters and derived sizes can be inspected before setup.
+static pt_status engine_create(Engine *s, const pt_params *params, const int *core_seeds, int K, void *cuda_stream)
+{
+    s->inst.resize(K);
+    for (int k = 0; k < K; k++) {
+        Instance &in = s->inst[k];
+        in.params = params[k];
+        in.core_seed = core_seeds[k];
+        in.rng.reset(new pth::GlibcRand((unsigned int)in.core_seed));
+        const char *why = nullptr;
+        pt_status st = pth::derive(in.params, in.core_seed, in.derived, *in.rng, &why);
+        if (st != PT_OK) {
+            std::string m = why ? why : "invalid parameters";
+            if (K > 1) m = "instance " + std::to_string(k) + ": " + m;
+            return fail(nullptr, st, m);
+        }
+        ptk::SimConst &c = in.c;
+        std::memset(&c, 0, sizeof(c));
+        c.H = in.derived.households;
+        c.L = in.derived.workplaces;
+        for (int t = 0; t < ptk::kTypes; t++) {
+            c.type_count[t] = in.derived.type_count[t];
+            c.type_offset[t] = in.derived.type_offset[t];
+        }
+        std::memcpy(c.shedding, in.derived.shedding, sizeof(c.shedding));
+        c.infectiousness[0] = in.derived.infectiousness[0];
+        c.infectiousness[1] = in.derived.infectiousness[1];
+        c.pct_sympt = in.params.percent_symptomatic;
+        c.key0 = in.derived.key0;
+        c.key1 = in.derived.key1;
+        if ((long long)c.L * 10 + 1 > 0x7FFFFFFFll) return fail(nullptr, PT_ERR_ARG, "too many locations");
+        in.counts.assign(ptk::kMaxDays * 16, 0);
+        in.infected.assign(ptk::kMaxDays, 0);
+        s->max_days = std::max(s->max_days, in.params.max_days);
     }
-    std::memcpy(c.shedding, s->derived.shedding, sizeof(c.shedding));
-    c.infectiousness[0] = s->derived.infectiousness[0];
-    c.infectiousness[1] = s->derived.infectiousness[1];
-    c.pct_sympt = params->percent_symptomatic;
-    c.key0 = s->derived.key0;
-    c.key1 = s->derived.key1;
-    if ((long long)c.L * 10 + 1 > 0x7FFFFFFFll) return fail(nullptr, PT_ERR_ARG, "too many locations");
-    // The CUDA stream and events are created by pt_setup, so parameters, seeds and
-    // scaling can be inspected without a device.
+    // The CUDA stream and events are created by setup.
     s->stream = (cudaStream_t)cuda_stream;
-    s->counts.assign(ptk::kMaxDays * 16, 0);
-    s->infected.assign(ptk::kMaxDays, 0);
-    *out = s.release();
     return PT_OK;
 }
 
-static pt_status reset_epidemic(pt_sim *s)
-{
-    const int N = s->c.N;
-    ptk::DevArrays &d = s->d;
-    CK(ptk::launch_init_status(N, d.state, d.gen_p, d.gen_s, d.claim, s->stream), "init_status");
-    const int P = s->params.initial_pandemic, S = s->params.initial_seasonal;
-    if (P + S > 0) {
-        CK(pt_memcpy(s, s->d_seeds, s->seed_list.data(), sizeof(int32_t) * (P + S), cudaMemcpyHostToDevice,
-                           s->stream), "seed copy");
-        CK(ptk::launch_seed_infected(s->d_seeds, P, S, d.state, d.gen_p, d.gen_s, s->stream), "seed");
-    }
-    ptk::Scalars z;
-    std::memset(&z, 0, sizeof(z));
-    // rand_offset after setup: H/4 (household types) + N/4 (workplaces)
-    z.rand_offset = (unsigned long long)(s->c.H / 4) + (unsigned long long)(N / 4);
-    z.adults = s->adults;
-    CK(pt_memcpy(s, d.sc, &z, sizeof(z), cudaMemcpyHostToDevice, s->stream), "scalars");
-    CK(cudaStreamSynchronize(s->stream), "reset sync");
-    s->day = 0;
-    s->stopped = false;
-    s->days_run = 0;
-    s->max_prop = 0.f;
-    s->max_prop_day = 0;
-    std::fill(s->counts.begin(), s->counts.end(), 0);
-    std::fill(s->infected.begin(), s->infected.end(), 0);
-    return PT_OK;
-}
+static pt_status engine_reset(Engine *s);
 
-pt_status pt_setup(pt_sim *s)
+// PandemicSim::setupSim (PandemicSim.cu:146-208) for every instance: population,
+// households, workplaces and schools, the workplace table, status arrays, initial
+// infected.  Household types and workplace draws run per instance (each has its own
+// counter stream); scans, the household scatter and the workplace table cover all
+// instances at once.
+static pt_status engine_setup(Engine *s)
 {
-    if (!s) return PT_ERR_ARG;
-    if (s->setup_done) return fail(s, PT_ERR_STATE, "pt_setup called twice");
+    if (s->setup_done) return fail(s, PT_ERR_STATE, "setup called twice");
     if (!s->stream) {
         CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         s->own_stream = true;
     }
-    ptk::SimConst &c = s->c;
-    const int H = c.H, L = c.L;
-    const long long maxN = 5ll * H;  // the largest household type holds 5 persons
-    const long long tiles_cap = std::max({maxN, 10ll * L + 1, (long long)H + 1}) / 4096 + 4;
-
-    // persistent small block: scalars, look-back tiles and control words, the
-    // generation histogram and the household offsets (H+1)
-    size_t small_bytes = round256(sizeof(ptk::Scalars)) + round256((tiles_cap + 4) * sizeof(unsigned long long)) +
-                         round256(512 * sizeof(int)) + round256(((size_t)H + 1) * 4);
-    CK(cudaMalloc(&s->small_mem, small_bytes), "cudaMalloc(small)");
-    Arena a0{s->small_mem, small_bytes, 0};
+    const int K = s->K();
     ptk::DevArrays &d = s->d;
+    // household slots (H + 1 per instance: the last holds its padding persons),
+    // locations and an upper bound of the persons
+    std::vector<int> hbase(K), lbase(K), bbase0(K), bbase1(K);
+    long long HS = 0, LT = 0, maxP = 0, B0 = 0, B1 = 0;
+    for (int k = 0; k < K; k++) {
+        const ptk::SimConst &c = s->inst[k].c;
+        hbase[k] = (int)HS;
+        lbase[k] = (int)LT;
+        bbase0[k] = (int)B0;
+        bbase1[k] = (int)B1;
+        HS += (long long)c.H + 1;
+        LT += c.L;
+        B0 += ptk::day_buckets(c, false);
+        B1 += ptk::day_buckets(c, true);
+        maxP += 5ll * c.H + ptk::kPersonTile;  // the largest household type holds 5 persons
+        if (HS + 1 > INT_MAX / 2 || LT + 2 > INT_MAX / 2 || B1 + 1 > INT_MAX / 2 || maxP > INT_MAX)
+            return fail(s, PT_ERR_ARG, "batch too large for 32-bit ids");
+    }
+    const long long Bday = std::max(B0, B1), Bmax = std::max(Bday, LT + 1);
+    const long long tiles_cap = std::max({maxP, Bmax + 1, HS + 1}) / 4096 + 4;
+
+    // small block: scalars, look-back tiles and control words, instance records and
+    // state, generation histograms, household offsets, setup counters
+    const size_t small_bytes = round256(sizeof(ptk::Scalars)) +
+                               round256((tiles_cap + 4) * sizeof(unsigned long long)) +
+                               round256((size_t)K * sizeof(ptk::InstConst)) + round256((size_t)K * sizeof(ptk::InstState)) +
+                               round256((size_t)K * 512 * sizeof(int)) + round256(((size_t)HS + 1) * 4) +
+                               round256((size_t)2 * K * sizeof(int));
+    CK(cudaMalloc(&s->small_mem, small_bytes), "cudaMalloc(small)");
+    s->small_bytes = small_bytes;
+    Arena a0{s->small_mem, small_bytes, 0};
     d.sc = a0.take<ptk::Scalars>(1);
     d.tiles = a0.take<unsigned long long>(tiles_cap + 4);
     d.tiles_cap = (int)tiles_cap;
-    s->d_hist = a0.take<int>(512);
-    d.hh_offset = a0.take<int32_t>((size_t)H + 1);
-    s->small_bytes = small_bytes;
+    ptk::InstConst *ic_dev = a0.take<ptk::InstConst>(K);
+    d.ic = ic_dev;
+    d.is = a0.take<ptk::InstState>(K);
+    s->d_hist = a0.take<int>((size_t)K * 512);
+    d.hh_offset = a0.take<int32_t>((size_t)HS + 1);
+    int *d_counts = a0.take<int>((size_t)2 * K);  // adults, persons per instance
     // setup-only block: household types and sizes
-    size_t setup_bytes = round256((size_t)H) + round256((size_t)H * 4);
+    const size_t setup_bytes = round256((size_t)HS) + round256((size_t)HS * 4);
     CK(cudaMalloc(&s->setup_mem, setup_bytes), "cudaMalloc(setup)");
     Arena a1{s->setup_mem, setup_bytes, 0};
-    uint8_t *types = a1.take<uint8_t>(H);
-    int32_t *sizes = a1.take<int32_t>(H);
+    uint8_t *types = a1.take<uint8_t>((size_t)HS);
+    int32_t *sizes = a1.take<int32_t>((size_t)HS);
     CK(cudaMemsetAsync(d.sc, 0, sizeof(ptk::Scalars), s->stream), "memset scalars");
     CK(cudaMemsetAsync(d.tiles, 0, (tiles_cap + 4) * sizeof(unsigned long long), s->stream), "memset tiles");
+    CK(cudaMemsetAsync(d_counts, 0, (size_t)2 * K * sizeof(int), s->stream), "memset counters");
     int *ctl = (int *)(d.tiles + tiles_cap);
 
-    // households: types and sizes, exclusive scan -> offsets and N
-    CK(ptk::launch_household_types(c, types, sizes, &d.sc->adults, s->stream), "household_types");
-    CK(ptk::launch_scan_exclusive(sizes, d.hh_offset, H, 0, d.tiles, ctl, &d.sc->error, nullptr, 0, nullptr,
+    // household types and sizes, persons and adults of each instance
+    for (int k = 0; k < K; k++)
+        CK(ptk::launch_household_types(s->inst[k].c, types + hbase[k], sizes + hbase[k], d_counts + k,
+                                       d_counts + K + k, s->stream), "household_types");
+    std::vector<int> hcounts((size_t)2 * K);
+    CK(pt_memcpy_sync(s, hcounts.data(), d_counts, hcounts.size() * sizeof(int), cudaMemcpyDeviceToHost),
+       "population counts");
+    long long P = 0;
+    std::vector<int> pbase(K);
+    for (int k = 0; k < K; k++) {
+        Instance &in = s->inst[k];
+        const int N = hcounts[K + k];
+        if (N <= 0) return fail(s, PT_ERR_STATE, "population is empty");
+        in.c.N = N;
+        in.adults = hcounts[k];
+        in.c.workplace_offset = (uint64_t)(in.c.H / 4);
+        if ((long long)in.params.initial_pandemic + in.params.initial_seasonal > N)
+            return fail(s, PT_ERR_ARG, "more initial infected than persons");
+        if ((long long)N * 3 >= (1ll << 30))
+            return fail(s, PT_ERR_ARG, "population too large (3N must stay below 2^30)");
+        pbase[k] = (int)P;
+        P += ((long long)N + ptk::kPersonTile - 1) / ptk::kPersonTile * ptk::kPersonTile;
+        s->persons += N;
+    }
+    if (3 * P >= (long long)INT_MAX) return fail(s, PT_ERR_ARG, "batch too large (3 x persons must stay below 2^31)");
+    s->ic.resize(K);
+    for (int k = 0; k < K; k++) {
+        ptk::InstConst &r = s->ic[k];
+        std::memset(&r, 0, sizeof(r));
+        r.c = s->inst[k].c;
+        r.pbase = pbase[k];
+        r.hbase = hbase[k];
+        r.lbase = lbase[k];
+        r.bbase[0] = bbase0[k];
+        r.bbase[1] = bbase1[k];
+        r.max_days = s->inst[k].params.max_days;
+        r.kbase = 3ll * pbase[k];
+    }
+    CK(pt_memcpy(s, ic_dev, s->ic.data(), (size_t)K * sizeof(ptk::InstConst), cudaMemcpyHostToDevice, s->stream),
+       "instance records");
+    d.K = K;
+    d.P = (int)P;
+    d.buckets[0] = (int)B0;
+    d.buckets[1] = (int)B1;
+    d.locations = (int)LT;
+    // padding slots, then one scan of all household slots: offsets and person bases
+    CK(ptk::launch_batch_padding(d, types, sizes, 0, false, s->stream), "padding slots");
+    CK(ptk::launch_scan_exclusive(sizes, d.hh_offset, (int)HS, 0, d.tiles, ctl, &d.sc->error, nullptr, 0, nullptr,
                                   s->stream), "household scan");
-    int hN = 0, hA = 0;
-    CK(pt_memcpy(s, &hN, d.hh_offset + H, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "N copy");
-    CK(pt_memcpy(s, &hA, &d.sc->adults, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "adults copy");
-    CK(cudaStreamSynchronize(s->stream), "setup sync");
-    if (hN <= 0) return fail(s, PT_ERR_STATE, "population is empty");
-    const int N = hN;
-    c.N = N;
-    s->adults = hA;
-    c.workplace_offset = (uint64_t)(H / 4);
-    const int P = s->params.initial_pandemic, S = s->params.initial_seasonal;
-    if ((long long)P + S > N) return fail(s, PT_ERR_ARG, "more initial infected than persons");
-
-    if ((long long)N * 3 >= (1ll << 30)) return fail(s, PT_ERR_ARG, "population too large (3N must stay below 2^30)");
 
     // arena of per-person and per-location arrays
-    const size_t n = (size_t)N, B = 10 * (size_t)L;
+    const size_t n = (size_t)P, ntiles = n / ptk::kPersonTile;
     const size_t radix_tiles = (3 * n + 4095) / 4096 + 1;
+    int nseeds = 0;
+    for (const Instance &in : s->inst) nseeds += in.params.initial_pandemic + in.params.initial_seasonal;
     size_t bytes = 0;
-    bytes += round256(n * 4);                 // state
-    bytes += 3 * round256(n);                 // gen_p, gen_s, age
-    bytes += round256(n * 4) * 3;             // household, workplace, wp_people
-    bytes += round256(((size_t)L + 1) * 4);   // wp_offset
-    bytes += round256(3 * n * 4) * 6;         // keys, bkt_people, radix k0/v0/k1/v1
-    bytes += round256((B + 1) * 4);           // bkt_offset
-    bytes += round256(B * 4);                 // bkt_count
-    bytes += round256(radix_tiles * 256 * 8); // radix look-back words
+    bytes += round256(n * 4);                   // state
+    bytes += 3 * round256(n);                   // gen_p, gen_s, age
+    bytes += round256(n * 4) * 3;               // household, workplace, wp_people
+    bytes += round256(((size_t)LT + 2) * 4);    // wp_offset
+    bytes += round256(3 * n * 4) * 6;           // keys, bkt_people, radix k0/v0/k1/v1
+    bytes += round256(((size_t)Bday + 1) * 4);  // bkt_offset
+    bytes += round256((size_t)Bmax * 4);        // bkt_count (also the workplace histogram)
+    bytes += round256(radix_tiles * 256 * 8);   // radix look-back words
     bytes += round256(8 * 4) + 2 * round256(4 * 256 * 4);  // radix ctl, digit hist/base
-    bytes += round256((B / 32 + 1) * 4);      // bucket mark bitmap
-    bytes += round256(n * 4);                 // infected
-    bytes += round256(2 * n * 8);             // claim
-    bytes += round256(2 * n * 4);             // new_list
-    bytes += round256((size_t)(P + S + 1) * 4);  // seeds
+    bytes += round256(((size_t)Bday / 32 + 1) * 4);        // bucket mark bitmap
+    bytes += round256(n * 4) * 2;               // infected, infected_inst
+    bytes += round256(2 * n * 8);               // claim
+    bytes += round256(2 * n * 4);               // new_list
+    bytes += round256((size_t)(nseeds + 1) * 4);  // seeds
+    bytes += round256(ntiles * 4);              // tile_inst
     CK(cudaMalloc(&s->arena_mem, bytes), "cudaMalloc(arena)");
     s->arena_bytes = bytes;
     Arena a{s->arena_mem, bytes, 0};
@@ -260,40 +337,57 @@ pt_status pt_setup(pt_sim *s)
     d.household = a.take<int32_t>(n);
     d.workplace = a.take<int32_t>(n);
     d.wp_people = a.take<int32_t>(n);
-    d.wp_offset = a.take<int32_t>((size_t)L + 1);
+    d.wp_offset = a.take<int32_t>((size_t)LT + 2);
     d.keys = a.take<int32_t>(3 * n);
     d.bkt_people = a.take<int32_t>(3 * n);
     d.rk0 = a.take<uint32_t>(3 * n);
     d.rv0 = a.take<uint32_t>(3 * n);
     d.rk1 = a.take<uint32_t>(3 * n);
     d.rv1 = a.take<uint32_t>(3 * n);
-    d.bkt_offset = a.take<int32_t>(B + 1);
-    d.bkt_count = a.take<int32_t>(B);
+    d.bkt_offset = a.take<int32_t>((size_t)Bday + 1);
+    d.bkt_count = a.take<int32_t>((size_t)Bmax);
     d.radix_status = a.take<unsigned long long>(radix_tiles * 256);
     d.radix_ctl = a.take<int>(8);
     d.digit_hist = a.take<int>(4 * 256);
     d.digit_base = a.take<int>(4 * 256);
-    d.mark = a.take<uint32_t>(B / 32 + 1);
+    d.mark = a.take<uint32_t>((size_t)Bday / 32 + 1);
     d.infected = a.take<int32_t>(n);
+    d.infected_inst = a.take<int32_t>(n);
     d.claim = a.take<unsigned long long>(2 * n);
     d.new_list = a.take<int32_t>(2 * n);
-    s->d_seeds = a.take<int32_t>((size_t)(P + S + 1));
-    CK(cudaMemsetAsync(d.bkt_count, 0, B * 4, s->stream), "memset counts");
+    s->d_seeds = a.take<int32_t>((size_t)(nseeds + 1));
+    int32_t *tile_inst = a.take<int32_t>(ntiles);
+    d.tile_inst = tile_inst;
+    {
+        std::vector<int32_t> ti(ntiles);
+        for (int k = 0; k < K; k++) {
+            const size_t t0 = (size_t)pbase[k] / ptk::kPersonTile;
+            const size_t t1 = k + 1 < K ? (size_t)pbase[k + 1] / ptk::kPersonTile : ntiles;
+            for (size_t t = t0; t < t1; t++) ti[t] = k;
+        }
+        CK(pt_memcpy(s, tile_inst, ti.data(), ntiles * 4, cudaMemcpyHostToDevice, s->stream), "tile map");
+        CK(cudaStreamSynchronize(s->stream), "tile map sync");
+    }
+    CK(cudaMemsetAsync(d.bkt_count, 0, (size_t)Bmax * 4, s->stream), "memset counts");
     CK(cudaMemsetAsync(d.radix_ctl, 0, 8 * 4, s->stream), "memset radix ctl");
     CK(cudaMemsetAsync(d.radix_status, 0, radix_tiles * 256 * 8, s->stream), "memset radix words");
     CK(cudaMemsetAsync(d.digit_hist, 0, 4 * 256 * 4, s->stream), "memset digit hist");
 
-    // households -> persons, then workplaces and schools (setup_assignWorkplaces)
-    CK(ptk::launch_generate_households(c, types, d.hh_offset, d.household, d.age, s->stream), "households");
-    CK(ptk::launch_assign_workplaces(c, d.age, d.workplace, s->stream), "workplaces");
+    // households -> persons, padding persons, then workplaces and schools (setup_assignWorkplaces)
+    CK(ptk::launch_generate_households(types, d.hh_offset, (int)HS, d.household, d.age, s->stream), "households");
+    CK(ptk::launch_batch_padding(d, types, sizes, (int)LT, true, s->stream), "padding persons");
+    for (int k = 0; k < K; k++)
+        CK(ptk::launch_assign_workplaces(s->inst[k].c, d.age + pbase[k], d.workplace + pbase[k], lbase[k], s->stream),
+           "workplaces");
     // workplace table: person ids stably sorted by workplace, with offsets
-    // (setup_assignWorkplaces' radix sort + lower_bound, PandemicSim.cu:3835-3862)
+    // (setup_assignWorkplaces' radix sort + lower_bound, PandemicSim.cu:3835-3862);
+    // padding persons sit in the spare location LT, behind every instance's persons
     {
         ptk::RadixArgs r;
         r.keys = (const uint32_t *)d.workplace;
-        r.E = N;
-        r.buckets = L;
-        r.N = N;
+        r.E = (int)P;
+        r.buckets = (int)LT + 1;
+        r.N = (int)P;
         r.person_mode = 0;
         r.k0 = d.rk0; r.v0 = d.rv0; r.k1 = d.rk1; r.v1 = d.rv1;
         r.out = (uint32_t *)d.wp_people;
@@ -305,55 +399,80 @@ pt_status pt_setup(pt_sim *s)
         CK(ptk::launch_bucket_table(r, d.bkt_count, true, d.wp_offset, d.tiles, ctl, d.digit_hist, s->stream),
            "workplace table");
     }
-    // initial infected: rand() % N draws continue the seed sequence (PandemicSim.cu:708-758)
-    s->seed_list = pth::unique_numbers(*s->rng, P + S, N);
+    // initial infected: rand() % N draws continue each instance's seed sequence
+    // (PandemicSim.cu:708-758); the first P of an instance get the pandemic strain
+    s->seed_global.clear();
+    std::vector<int32_t> seasonal;
+    for (int k = 0; k < K; k++) {
+        Instance &in = s->inst[k];
+        const int np = in.params.initial_pandemic, ns = in.params.initial_seasonal;
+        in.seed_list = pth::unique_numbers(*in.rng, np + ns, in.c.N);
+        for (int i = 0; i < np + ns; i++) (i < np ? s->seed_global : seasonal).push_back(pbase[k] + in.seed_list[i]);
+    }
+    s->seeds_p = (int)s->seed_global.size();
+    s->seeds_s = (int)seasonal.size();
+    s->seed_global.insert(s->seed_global.end(), seasonal.begin(), seasonal.end());
     int derr = 0;
     CK(pt_memcpy(s, &derr, &d.sc->error, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "error flag");
     CK(cudaStreamSynchronize(s->stream), "setup sync");
     cudaFree(s->setup_mem);
     s->setup_mem = nullptr;
     if (derr) return fail(s, PT_ERR_TIMEOUT, "a device-side wait gave up during setup");
-    pt_status st = reset_epidemic(s);
+    pt_status st = engine_reset(s);
     if (st != PT_OK) return st;
     s->setup_done = true;
     return PT_OK;
 }
 
-pt_status pt_reset_epidemic(pt_sim *s)
+static pt_status engine_reset(Engine *s)
 {
-    if (!s) return PT_ERR_ARG;
-    if (!s->setup_done) return fail(s, PT_ERR_STATE, "pt_reset_epidemic before pt_setup");
-    return reset_epidemic(s);
+    ptk::DevArrays &d = s->d;
+    CK(ptk::launch_init_status(d.P, d.state, d.gen_p, d.gen_s, d.claim, s->stream), "init_status");
+    if (!s->seed_global.empty()) {
+        CK(pt_memcpy(s, s->d_seeds, s->seed_global.data(), sizeof(int32_t) * s->seed_global.size(),
+                     cudaMemcpyHostToDevice, s->stream), "seed copy");
+        CK(ptk::launch_seed_infected(s->d_seeds, s->seeds_p, s->seeds_s, d.state, d.gen_p, d.gen_s, s->stream), "seed");
+    }
+    CK(cudaMemsetAsync(d.sc, 0, sizeof(ptk::Scalars), s->stream), "memset scalars");
+    CK(ptk::launch_reset_instances(d, s->stream), "reset instances");
+    CK(cudaStreamSynchronize(s->stream), "reset sync");
+    s->next_day = 0;
+    for (Instance &in : s->inst) {
+        in.day = 0;
+        in.stopped = false;
+        in.days_run = 0;
+        in.max_prop = 0.f;
+        in.max_prop_day = 0;
+        std::fill(in.counts.begin(), in.counts.end(), 0);
+        std::fill(in.infected.begin(), in.infected.end(), 0);
+    }
+    return PT_OK;
 }
 
-// Stage boundaries recorded per day when timing is on.
-enum { kStSweep, kStSchedule, kStScan, kStRadix, kStInfect, kStApply, kStages };
-
-static cudaEvent_t stage_event(pt_sim *s, int day, int k)
+static cudaEvent_t stage_event(Engine *s, int day, int k)
 {
     return s->day_events[(size_t)day * (kStages + 1) + k];
 }
 
-// Enqueues one day: sweep, schedule, bucket build (scan, radix sort), infection,
-// apply.  Every kernel after the sweep skips itself on the device when the day
-// counted no infected.
-static pt_status enqueue_day(pt_sim *s, int day)
+// Enqueues one day of every instance: sweep, schedule, bucket build (scan, radix
+// sort), infection, apply.  Every kernel after the sweep skips an instance that
+// counted no infected, and skips itself once no instance has infected left.
+static pt_status enqueue_day(Engine *s, int day)
 {
     const bool weekend = (day % 7) >= 5;  // PandemicSim.h:283-284
-    const ptk::SimConst &c = s->c;
     const ptk::DevArrays &d = s->d;
     cudaStream_t st = s->stream;
     const bool t = s->timing;
     if (t) cudaEventRecord(stage_event(s, day, 0), st);
-    CK(ptk::launch_sweep(c, d, day, st), "sweep");
+    CK(ptk::launch_sweep(d, day, st), "sweep");
     if (t) cudaEventRecord(stage_event(s, day, 1), st);
-    CK(ptk::launch_schedule(c, d, weekend, s->full_tables, st), "schedule");
+    CK(ptk::launch_schedule(d, weekend, day, s->full_tables, st), "schedule");
     if (t) cudaEventRecord(stage_event(s, day, 2), st);
-    CK(ptk::launch_bucket_scan(c, d, weekend, st), "bucket scan");
+    CK(ptk::launch_bucket_scan(d, weekend, st), "bucket scan");
     if (t) cudaEventRecord(stage_event(s, day, 3), st);
-    CK(ptk::launch_bucket_sort(c, d, weekend, st), "bucket sort");
+    CK(ptk::launch_bucket_sort(d, weekend, st), "bucket sort");
     if (t) cudaEventRecord(stage_event(s, day, 4), st);
-    CK(ptk::launch_infect(c, d, weekend, day, st), "infect");
+    CK(ptk::launch_infect(d, weekend, day, st), "infect");
     if (t) cudaEventRecord(stage_event(s, day, 5), st);
     CK(ptk::launch_apply(d, day, st), "apply");
     if (t) cudaEventRecord(stage_event(s, day, 6), st);
@@ -361,7 +480,7 @@ static pt_status enqueue_day(pt_sim *s, int day)
     return PT_OK;
 }
 
-static void accumulate_timing(pt_sim *s)
+static void accumulate_timing(Engine *s)
 {
     if (!s->timing) return;
     cudaStreamSynchronize(s->stream);
@@ -377,62 +496,99 @@ static void accumulate_timing(pt_sim *s)
     s->timed_days.clear();
 }
 
-static pt_status check_device_error(pt_sim *s)
+static void track_peak(Engine *s, Instance &in, int day, int I)
 {
+    (void)s;
+    // PandemicSim.cu:923-931: strictly greater proportions only
+    float prop = (float)I / (float)in.c.N;
+    if (prop > in.max_prop) {
+        in.max_prop = prop;
+        in.max_prop_day = day;
+    }
+}
+
+// Copies every instance's rows of days [lo, hi) (strided copies out of the device
+// state records), checks the device error word and updates the host mirrors.
+static pt_status fetch_rows(Engine *s, int lo, int hi)
+{
+    const int K = s->K();
+    const size_t pitch = sizeof(ptk::InstState);
+    const int days = std::max(0, hi - lo);
+    std::vector<int> hc((size_t)K * 16 * std::max(days, 1)), hi_((size_t)K * std::max(days, 1)), rows(K);
+    char *base = reinterpret_cast<char *>(s->d.is);
+    if (days > 0) {
+        const size_t wc = (size_t)days * 16 * sizeof(int), wi = (size_t)days * sizeof(int);
+        s->d2h_bytes += (uint64_t)K * (wc + wi);
+        CK(cudaMemcpy2DAsync(hc.data(), wc, base + offsetof(ptk::InstState, counts) + (size_t)lo * 16 * sizeof(int),
+                             pitch, wc, K, cudaMemcpyDeviceToHost, s->stream), "counts");
+        CK(cudaMemcpy2DAsync(hi_.data(), wi, base + offsetof(ptk::InstState, infected_per_day) + (size_t)lo * sizeof(int),
+                             pitch, wi, K, cudaMemcpyDeviceToHost, s->stream), "infected");
+    }
+    s->d2h_bytes += (uint64_t)K * sizeof(int);
+    CK(cudaMemcpy2DAsync(rows.data(), sizeof(int), base + offsetof(ptk::InstState, days_run), pitch, sizeof(int), K,
+                         cudaMemcpyDeviceToHost, s->stream), "rows");
     int e = 0;
     CK(pt_memcpy(s, &e, &s->d.sc->error, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "error flag");
     CK(cudaStreamSynchronize(s->stream), "sync");
     if (e) return fail(s, PT_ERR_TIMEOUT, "a device-side wait gave up (look-back ordering)");
+    accumulate_timing(s);
+    for (int k = 0; k < K; k++) {
+        Instance &in = s->inst[k];
+        if (in.stopped) continue;
+        for (int day = in.days_run; day < rows[k]; day++) {
+            if (day < lo || day >= hi) continue;  // outside the rows copied
+            const size_t r = (size_t)k * days + (day - lo);
+            std::memcpy(&in.counts[(size_t)day * 16], &hc[r * 16], 16 * sizeof(int));
+            in.infected[day] = hi_[r];
+            if (hi_[r] == 0) {
+                in.stopped = true;
+                break;
+            }
+            track_peak(s, in, day, hi_[r]);
+        }
+        in.days_run = rows[k];
+        in.day = in.stopped ? rows[k] - 1 : rows[k];
+    }
     return PT_OK;
 }
 
-static void track_peak(pt_sim *s, int day, int I)
+static int instances_running(const Engine *s)
 {
-    // PandemicSim.cu:923-931: strictly greater proportions only
-    float prop = (float)I / (float)s->c.N;
-    if (prop > s->max_prop) {
-        s->max_prop = prop;
-        s->max_prop_day = day;
-    }
+    int n = 0;
+    for (const Instance &in : s->inst)
+        if (!in.stopped && in.day < in.params.max_days) n++;
+    return n;
 }
 
-pt_status pt_step_day(pt_sim *s, int counts16[16], int *infected_count)
+static bool all_zero_stopped(const Engine *s)
 {
-    if (!s) return PT_ERR_ARG;
-    if (!s->setup_done) return fail(s, PT_ERR_STATE, "pt_step_day before pt_setup");
-    if (s->stopped) return PT_DONE;
-    if (s->day >= s->params.max_days) return PT_FINISHED;
-    const int day = s->day;
+    for (const Instance &in : s->inst)
+        if (!in.stopped) return false;
+    return true;
+}
+
+// One day of every running instance (runToCompletion's loop body, PandemicSim.cu:882-954).
+static pt_status engine_step(Engine *s, int *running)
+{
+    if (!s->setup_done) return fail(s, PT_ERR_STATE, "step before setup");
+    if (instances_running(s) == 0) return all_zero_stopped(s) ? PT_DONE : PT_FINISHED;
+    const int day = s->next_day;
     pt_status st = enqueue_day(s, day);
     if (st != PT_OK) return st;
-    int buf[17];
-    CK(pt_memcpy(s, buf, s->d.sc->counts[day], 16 * sizeof(int), cudaMemcpyDeviceToHost, s->stream), "counts");
-    CK(pt_memcpy(s, buf + 16, &s->d.sc->infected_per_day[day], sizeof(int), cudaMemcpyDeviceToHost, s->stream),
-       "infected");
-    st = check_device_error(s);
+    s->next_day = day + 1;
+    st = fetch_rows(s, day, day + 1);
     if (st != PT_OK) return st;
-    accumulate_timing(s);
-    std::memcpy(&s->counts[day * 16], buf, 16 * sizeof(int));
-    s->infected[day] = buf[16];
-    if (counts16) std::memcpy(counts16, buf, 16 * sizeof(int));
-    if (infected_count) *infected_count = buf[16];
-    s->days_run = day + 1;
-    if (buf[16] == 0) {
-        s->stopped = true;
-        return PT_DONE;
-    }
-    track_peak(s, day, buf[16]);
-    s->day = day + 1;
-    return PT_OK;
+    if (running) *running = instances_running(s);
+    return all_zero_stopped(s) ? PT_DONE : PT_OK;
 }
 
-pt_status pt_run(pt_sim *s, int *counts, int *infected, int *days_run)
+// The remaining days of every instance on the device, then one copy of the rows.
+static pt_status engine_run(Engine *s)
 {
-    if (!s) return PT_ERR_ARG;
-    if (!s->setup_done) return fail(s, PT_ERR_STATE, "pt_run before pt_setup");
-    const int first = s->day, M = s->params.max_days;
-    if (!s->stopped) {
-        if (first == 0 && !s->timing && M > 0) {
+    if (!s->setup_done) return fail(s, PT_ERR_STATE, "run before setup");
+    const int first = s->next_day, M = s->max_days;
+    if (instances_running(s) > 0 && first < M) {
+        if (first == 0 && !s->timing) {
             if (!s->run_graph) {
                 const uint64_t before = ptk::launches();
                 CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
@@ -459,96 +615,72 @@ pt_status pt_run(pt_sim *s, int *counts, int *infected, int *days_run)
                 if (st != PT_OK) return st;
             }
         }
+        s->next_day = M;
     }
-    // one copy of all per-day results
-    std::vector<int> hc(ptk::kMaxDays * 16), hi(ptk::kMaxDays);
-    int rows = 0;
-    CK(pt_memcpy(s, hc.data(), s->d.sc->counts, hc.size() * sizeof(int), cudaMemcpyDeviceToHost, s->stream),
-       "counts");
-    CK(pt_memcpy(s, hi.data(), s->d.sc->infected_per_day, hi.size() * sizeof(int), cudaMemcpyDeviceToHost,
-                       s->stream), "infected");
-    CK(pt_memcpy(s, &rows, &s->d.sc->days_run, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "rows");
-    pt_status st = check_device_error(s);
-    if (st != PT_OK) return st;
-    accumulate_timing(s);
-    if (!s->stopped) {
-        for (int day = first; day < rows; day++) {
-            std::memcpy(&s->counts[day * 16], &hc[day * 16], 16 * sizeof(int));
-            s->infected[day] = hi[day];
-            if (hi[day] == 0) {
-                s->stopped = true;
-                break;
-            }
-            track_peak(s, day, hi[day]);
-        }
-        s->days_run = rows;
-        s->day = s->stopped ? rows - 1 : rows;
+    return fetch_rows(s, first, std::max(first, M));
+}
+
+static pt_status engine_gen_counts(Engine *s, int *gen_p, int *gen_s)
+{
+    if (!s->setup_done) return fail(s, PT_ERR_STATE, "generation counts before setup");
+    const int K = s->K();
+    CK(ptk::launch_gen_hist(s->d, s->d_hist, s->stream), "gen hist");
+    std::vector<int> h((size_t)K * 512);
+    CK(pt_memcpy_sync(s, h.data(), s->d_hist, h.size() * sizeof(int), cudaMemcpyDeviceToHost), "hist copy");
+    for (int k = 0; k < K; k++) {
+        std::memcpy(gen_p + (size_t)k * 256, &h[(size_t)k * 512], 256 * sizeof(int));
+        std::memcpy(gen_s + (size_t)k * 256, &h[(size_t)k * 512 + 256], 256 * sizeof(int));
     }
-    if (counts) std::memcpy(counts, s->counts.data(), (size_t)s->days_run * 16 * sizeof(int));
-    if (infected) std::memcpy(infected, s->infected.data(), (size_t)s->days_run * sizeof(int));
-    if (days_run) *days_run = s->days_run;
     return PT_OK;
 }
 
-pt_status pt_final_gen_counts(pt_sim *s, int gen_p[256], int gen_s[256])
+static pt_status engine_info(const Engine *cs, int k, pt_info *out)
 {
-    if (!s || !gen_p || !gen_s) return PT_ERR_ARG;
-    if (!s->setup_done) return fail(s, PT_ERR_STATE, "pt_final_gen_counts before pt_setup");
-    CK(ptk::launch_gen_hist(s->d.gen_p, s->d.gen_s, s->c.N, s->d_hist, s->stream), "gen hist");
-    int h[512];
-    CK(pt_memcpy(s, h, s->d_hist, sizeof(h), cudaMemcpyDeviceToHost, s->stream), "hist copy");
-    CK(cudaStreamSynchronize(s->stream), "sync");
-    std::memcpy(gen_p, h, 256 * sizeof(int));
-    std::memcpy(gen_s, h + 256, 256 * sizeof(int));
-    return PT_OK;
-}
-
-pt_status pt_get_info(const pt_sim *s, pt_info *out)
-{
-    if (!s || !out) return PT_ERR_ARG;
+    Engine *s = const_cast<Engine *>(cs);
     std::memset(out, 0, sizeof(*out));
-    out->number_people = s->c.N;
-    out->number_households = s->c.H;
-    out->number_workplaces = s->c.L;
-    out->number_adults = s->adults;
-    out->number_children = s->c.N - s->adults;
-    out->current_day = s->day;
-    out->days_run = s->days_run;
-    out->infected_count = s->days_run > 0 ? s->infected[s->days_run - 1] : 0;
-    for (int i = 0; i < 4; i++) out->seeds[i] = s->derived.seeds[i];
-    for (int t = 0; t < 14; t++) {
-        out->type_count[t] = s->c.type_count[t];
-        out->type_offset[t] = s->c.type_offset[t];
+    const Instance &in = s->inst[k];
+    out->number_people = in.c.N;
+    out->number_households = in.c.H;
+    out->number_workplaces = in.c.L;
+    out->number_adults = in.adults;
+    out->number_children = in.c.N - in.adults;
+    out->current_day = in.day;
+    out->days_run = in.days_run;
+    out->infected_count = in.days_run > 0 ? in.infected[in.days_run - 1] : 0;
+    for (int i = 0; i < 4; i++) out->seeds[i] = in.derived.seeds[i];
+    for (int t = 0; t < ptk::kTypes; t++) {
+        out->type_count[t] = in.c.type_count[t];
+        out->type_offset[t] = in.c.type_offset[t];
     }
-    out->infectiousness[0] = s->c.infectiousness[0];
-    out->infectiousness[1] = s->c.infectiousness[1];
-    out->max_day_of_peak = s->max_prop_day;
-    out->max_infected_proportion = s->max_prop;
+    out->infectiousness[0] = in.c.infectiousness[0];
+    out->infectiousness[1] = in.c.infectiousness[1];
+    out->max_day_of_peak = in.max_prop_day;
+    out->max_infected_proportion = in.max_prop;
     out->sm_count = ptk::sm_count();
     out->device_bytes = s->arena_bytes + s->small_bytes;
     if (s->setup_done) {
-        unsigned long long v[2] = {0, 0};
-        pt_memcpy_sync(s, v, &s->d.sc->rand_offset, sizeof(v), cudaMemcpyDeviceToHost);
-        out->rand_offset = v[0];
-        out->bucket_entries_materialised = v[1];
+        unsigned long long ro = 0, mat = 0;
+        CK(pt_memcpy(s, &ro, &s->d.is[k].rand_offset, sizeof(ro), cudaMemcpyDeviceToHost, s->stream), "offset");
+        CK(pt_memcpy_sync(s, &mat, &s->d.sc->materialised_sum, sizeof(mat), cudaMemcpyDeviceToHost), "materialised");
+        out->rand_offset = ro;
+        out->bucket_entries_materialised = mat;  // over all instances of the engine
         uint64_t total = 0;
-        for (int day = 0; day < s->days_run; day++)
-            if (s->infected[day] > 0) total += (uint64_t)((day % 7) >= 5 ? 3 : 2) * (uint64_t)s->c.N;
+        for (int day = 0; day < in.days_run; day++)
+            if (in.infected[day] > 0) total += (uint64_t)((day % 7) >= 5 ? 3 : 2) * (uint64_t)in.c.N;
         out->bucket_entries_scheduled = total;
     }
     return PT_OK;
 }
 
-pt_status pt_get_person_state(pt_sim *s, uint8_t *status_p, uint8_t *status_s, uint8_t *day_p, uint8_t *day_s,
-                              uint8_t *gen_p, uint8_t *gen_s, uint8_t *age)
+static pt_status engine_person_state(Engine *s, int k, uint8_t *status_p, uint8_t *status_s, uint8_t *day_p,
+                                     uint8_t *day_s, uint8_t *gen_p, uint8_t *gen_s, uint8_t *age)
 {
-    if (!s) return PT_ERR_ARG;
-    if (!s->setup_done) return fail(s, PT_ERR_STATE, "state before pt_setup");
-    const size_t N = (size_t)s->c.N;
+    if (!s->setup_done) return fail(s, PT_ERR_STATE, "state before setup");
+    const size_t N = (size_t)s->inst[k].c.N, pb = (size_t)s->ic[k].pbase;
     CK(cudaStreamSynchronize(s->stream), "sync");
     if (status_p || status_s || day_p || day_s) {
         std::vector<uint32_t> st(N);
-        CK(pt_memcpy_sync(s, st.data(), s->d.state, N * 4, cudaMemcpyDeviceToHost), "state copy");
+        CK(pt_memcpy_sync(s, st.data(), s->d.state + pb, N * 4, cudaMemcpyDeviceToHost), "state copy");
         for (size_t i = 0; i < N; i++) {
             if (status_p) status_p[i] = (uint8_t)(st[i] & 0xFF);
             if (status_s) status_s[i] = (uint8_t)((st[i] >> 8) & 0xFF);
@@ -556,10 +688,150 @@ pt_status pt_get_person_state(pt_sim *s, uint8_t *status_p, uint8_t *status_s, u
             if (day_s) day_s[i] = (uint8_t)(st[i] >> 24);
         }
     }
-    if (gen_p) CK(pt_memcpy_sync(s, gen_p, s->d.gen_p, N, cudaMemcpyDeviceToHost), "gen copy");
-    if (gen_s) CK(pt_memcpy_sync(s, gen_s, s->d.gen_s, N, cudaMemcpyDeviceToHost), "gen copy");
-    if (age) CK(pt_memcpy_sync(s, age, s->d.age, N, cudaMemcpyDeviceToHost), "age copy");
+    if (gen_p) CK(pt_memcpy_sync(s, gen_p, s->d.gen_p + pb, N, cudaMemcpyDeviceToHost), "gen copy");
+    if (gen_s) CK(pt_memcpy_sync(s, gen_s, s->d.gen_s + pb, N, cudaMemcpyDeviceToHost), "gen copy");
+    if (age) CK(pt_memcpy_sync(s, age, s->d.age + pb, N, cudaMemcpyDeviceToHost), "age copy");
     return PT_OK;
+}
+
+// Setup tables of instance k in its own numbering (global ids minus its bases).
+static pt_status engine_population(Engine *s, int k, int32_t *household, int32_t *household_offset,
+                                   int32_t *workplace, int32_t *workplace_people, int32_t *workplace_offset)
+{
+    if (!s->setup_done) return fail(s, PT_ERR_STATE, "population before setup");
+    const ptk::InstConst &r = s->ic[k];
+    const size_t N = (size_t)r.c.N, H = (size_t)r.c.H, L = (size_t)r.c.L;
+    CK(cudaStreamSynchronize(s->stream), "sync");
+    auto rebase = [](int32_t *v, size_t n, int32_t by) {
+        if (by)
+            for (size_t i = 0; i < n; i++) v[i] -= by;
+    };
+    if (household) {
+        CK(pt_memcpy_sync(s, household, s->d.household + r.pbase, N * 4, cudaMemcpyDeviceToHost), "copy");
+        rebase(household, N, r.hbase);
+    }
+    if (household_offset) {
+        CK(pt_memcpy_sync(s, household_offset, s->d.hh_offset + r.hbase, (H + 1) * 4, cudaMemcpyDeviceToHost), "copy");
+        rebase(household_offset, H + 1, r.pbase);
+    }
+    if (workplace) {
+        CK(pt_memcpy_sync(s, workplace, s->d.workplace + r.pbase, N * 4, cudaMemcpyDeviceToHost), "copy");
+        rebase(workplace, N, r.lbase);
+    }
+    if (workplace_people || workplace_offset) {
+        std::vector<int32_t> off(L + 1);
+        CK(pt_memcpy_sync(s, off.data(), s->d.wp_offset + r.lbase, (L + 1) * 4, cudaMemcpyDeviceToHost), "copy");
+        const int32_t first = off[0];
+        if (workplace_people) {
+            CK(pt_memcpy_sync(s, workplace_people, s->d.wp_people + first, N * 4, cudaMemcpyDeviceToHost), "copy");
+            rebase(workplace_people, N, r.pbase);
+        }
+        if (workplace_offset) {
+            for (size_t i = 0; i <= L; i++) workplace_offset[i] = off[i] - first;
+        }
+    }
+    return PT_OK;
+}
+
+static pt_status engine_set_timing(Engine *s, int enabled)
+{
+    if (enabled && s->day_events.empty()) {
+        s->day_events.resize((size_t)ptk::kMaxDays * (kStages + 1));
+        for (auto &e : s->day_events) CK(cudaEventCreate(&e), "cudaEventCreate");
+    }
+    s->timing = enabled != 0;
+    std::memset(s->stage_ms, 0, sizeof(s->stage_ms));
+    s->stage_days[0] = s->stage_days[1] = 0;
+    return PT_OK;
+}
+
+static pt_status engine_stage_ms(Engine *s, float ms[16], int days[2])
+{
+    accumulate_timing(s);
+    std::memcpy(ms, s->stage_ms, sizeof(s->stage_ms));
+    if (days) {
+        days[0] = s->stage_days[0];
+        days[1] = s->stage_days[1];
+    }
+    std::memset(s->stage_ms, 0, sizeof(s->stage_ms));
+    s->stage_days[0] = s->stage_days[1] = 0;
+    return PT_OK;
+}
+
+extern "C" {
+
+// ------------------------------------------------------------------ one simulation
+pt_status pt_create(const pt_params *params, int core_seed, void *cuda_stream, pt_sim **out)
+{
+    if (!params || !out) return fail(nullptr, PT_ERR_ARG, "null argument");
+    *out = nullptr;
+    std::unique_ptr<pt_sim> s(new pt_sim());
+    pt_status st = engine_create(s.get(), params, &core_seed, 1, cuda_stream);
+    if (st != PT_OK) return st;
+    *out = s.release();
+    return PT_OK;
+}
+
+pt_status pt_setup(pt_sim *s)
+{
+    if (!s) return PT_ERR_ARG;
+    if (s->setup_done) return fail(s, PT_ERR_STATE, "pt_setup called twice");
+    return engine_setup(s);
+}
+
+pt_status pt_reset_epidemic(pt_sim *s)
+{
+    if (!s) return PT_ERR_ARG;
+    if (!s->setup_done) return fail(s, PT_ERR_STATE, "pt_reset_epidemic before pt_setup");
+    return engine_reset(s);
+}
+
+pt_status pt_step_day(pt_sim *s, int counts16[16], int *infected_count)
+{
+    if (!s) return PT_ERR_ARG;
+    if (!s->setup_done) return fail(s, PT_ERR_STATE, "pt_step_day before pt_setup");
+    const Instance &in = s->inst[0];
+    const int day = in.day;
+    const bool ran = !in.stopped && day < in.params.max_days;
+    pt_status st = engine_step(s, nullptr);
+    if (!ran || st < 0) return st;
+    if (counts16) std::memcpy(counts16, &in.counts[(size_t)day * 16], 16 * sizeof(int));
+    if (infected_count) *infected_count = in.infected[day];
+    return st;
+}
+
+pt_status pt_run(pt_sim *s, int *counts, int *infected, int *days_run)
+{
+    if (!s) return PT_ERR_ARG;
+    if (!s->setup_done) return fail(s, PT_ERR_STATE, "pt_run before pt_setup");
+    pt_status st = engine_run(s);
+    if (st != PT_OK) return st;
+    const Instance &in = s->inst[0];
+    if (counts) std::memcpy(counts, in.counts.data(), (size_t)in.days_run * 16 * sizeof(int));
+    if (infected) std::memcpy(infected, in.infected.data(), (size_t)in.days_run * sizeof(int));
+    if (days_run) *days_run = in.days_run;
+    return PT_OK;
+}
+
+pt_status pt_final_gen_counts(pt_sim *s, int gen_p[256], int gen_s[256])
+{
+    if (!s || !gen_p || !gen_s) return PT_ERR_ARG;
+    if (!s->setup_done) return fail(s, PT_ERR_STATE, "pt_final_gen_counts before pt_setup");
+    return engine_gen_counts(s, gen_p, gen_s);
+}
+
+pt_status pt_get_info(const pt_sim *s, pt_info *out)
+{
+    if (!s || !out) return PT_ERR_ARG;
+    return engine_info(s, 0, out);
+}
+
+pt_status pt_get_person_state(pt_sim *s, uint8_t *status_p, uint8_t *status_s, uint8_t *day_p, uint8_t *day_s,
+                              uint8_t *gen_p, uint8_t *gen_s, uint8_t *age)
+{
+    if (!s) return PT_ERR_ARG;
+    if (!s->setup_done) return fail(s, PT_ERR_STATE, "state before pt_setup");
+    return engine_person_state(s, 0, status_p, status_s, day_p, day_s, gen_p, gen_s, age);
 }
 
 pt_status pt_get_population(pt_sim *s, int32_t *household, int32_t *household_offset, int32_t *workplace,
@@ -567,16 +839,7 @@ pt_status pt_get_population(pt_sim *s, int32_t *household, int32_t *household_of
 {
     if (!s) return PT_ERR_ARG;
     if (!s->setup_done) return fail(s, PT_ERR_STATE, "population before pt_setup");
-    const size_t N = (size_t)s->c.N;
-    CK(cudaStreamSynchronize(s->stream), "sync");
-    if (household) CK(pt_memcpy_sync(s, household, s->d.household, N * 4, cudaMemcpyDeviceToHost), "copy");
-    if (household_offset)
-        CK(pt_memcpy_sync(s, household_offset, s->d.hh_offset, ((size_t)s->c.H + 1) * 4, cudaMemcpyDeviceToHost), "copy");
-    if (workplace) CK(pt_memcpy_sync(s, workplace, s->d.workplace, N * 4, cudaMemcpyDeviceToHost), "copy");
-    if (workplace_people) CK(pt_memcpy_sync(s, workplace_people, s->d.wp_people, N * 4, cudaMemcpyDeviceToHost), "copy");
-    if (workplace_offset)
-        CK(pt_memcpy_sync(s, workplace_offset, s->d.wp_offset, ((size_t)s->c.L + 1) * 4, cudaMemcpyDeviceToHost), "copy");
-    return PT_OK;
+    return engine_population(s, 0, household, household_offset, workplace, workplace_people, workplace_offset);
 }
 
 // The device keeps each day's buckets in compact form: errand destinations of a
@@ -591,18 +854,20 @@ pt_status pt_get_day_tables(pt_sim *s, int32_t *infected, int32_t *keys, int32_t
     if (!s) return PT_ERR_ARG;
     if (!s->setup_done) return fail(s, PT_ERR_STATE, "tables before pt_setup");
     CK(cudaStreamSynchronize(s->stream), "sync");
-    ptk::Scalars sc;
-    CK(pt_memcpy_sync(s, &sc, s->d.sc, sizeof(sc), cudaMemcpyDeviceToHost), "scalars");
-    const int day = sc.day;
+    int dayinf[2] = {0, 0};
+    CK(pt_memcpy(s, &dayinf[0], &s->d.is[0].day, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "day");
+    CK(pt_memcpy_sync(s, &dayinf[1], &s->d.is[0].infected, sizeof(int), cudaMemcpyDeviceToHost), "infected");
+    const int day = dayinf[0], I = dayinf[1];
     const bool weekend = (day % 7) >= 5;
-    const int L = s->c.L, hours = weekend ? 10 : 2;
-    const int lo = s->c.type_offset[weekend ? 9 : 8], R = L - lo;
-    const int E = (weekend ? 3 : 2) * s->c.N, B = hours * L;
-    const int Bc = ptk::day_buckets(s->c, weekend);
+    const ptk::SimConst &c = s->inst[0].c;
+    const int L = c.L, hours = weekend ? 10 : 2;
+    const int lo = c.type_offset[weekend ? 9 : 8], R = L - lo;
+    const int E = (weekend ? 3 : 2) * c.N, B = hours * L;
+    const int Bc = ptk::day_buckets(c, weekend);
     if (entries) *entries = E;
     if (buckets) *buckets = B;
-    if (infected && sc.infected > 0)
-        CK(pt_memcpy_sync(s, infected, s->d.infected, (size_t)sc.infected * 4, cudaMemcpyDeviceToHost), "copy");
+    if (infected && I > 0)
+        CK(pt_memcpy_sync(s, infected, s->d.infected, (size_t)I * 4, cudaMemcpyDeviceToHost), "copy");
     if (keys) {
         CK(pt_memcpy_sync(s, keys, s->d.keys, (size_t)E * 4, cudaMemcpyDeviceToHost), "copy");
         for (int i = 0; i < E; i++) {
@@ -638,28 +903,13 @@ pt_status pt_set_full_tables(pt_sim *s, int enabled)
 pt_status pt_set_timing(pt_sim *s, int enabled)
 {
     if (!s) return PT_ERR_ARG;
-    if (enabled && s->day_events.empty()) {
-        s->day_events.resize((size_t)ptk::kMaxDays * (kStages + 1));
-        for (auto &e : s->day_events) CK(cudaEventCreate(&e), "cudaEventCreate");
-    }
-    s->timing = enabled != 0;
-    std::memset(s->stage_ms, 0, sizeof(s->stage_ms));
-    s->stage_days[0] = s->stage_days[1] = 0;
-    return PT_OK;
+    return engine_set_timing(s, enabled);
 }
 
 pt_status pt_get_stage_ms(pt_sim *s, float ms[16], int days[2])
 {
     if (!s || !ms) return PT_ERR_ARG;
-    accumulate_timing(s);
-    std::memcpy(ms, s->stage_ms, sizeof(s->stage_ms));
-    if (days) {
-        days[0] = s->stage_days[0];
-        days[1] = s->stage_days[1];
-    }
-    std::memset(s->stage_ms, 0, sizeof(s->stage_ms));
-    s->stage_days[0] = s->stage_days[1] = 0;
-    return PT_OK;
+    return engine_stage_ms(s, ms, days);
 }
 
 uint64_t pt_launch_count(void) { return ptk::launches(); }
@@ -672,24 +922,127 @@ pt_status pt_transfer_bytes(const pt_sim *s, uint64_t *h2d, uint64_t *d2h)
     return PT_OK;
 }
 
-void pt_destroy(pt_sim *s)
-{
-    if (!s) return;
-    if (s->stream) cudaStreamSynchronize(s->stream);
-    if (s->run_graph) cudaGraphExecDestroy(s->run_graph);
-    cudaFree(s->arena_mem);
-    cudaFree(s->setup_mem);
-    cudaFree(s->small_mem);
-    for (auto &e : s->day_events)
-        if (e) cudaEventDestroy(e);
-    if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
-    delete s;
-}
+void pt_destroy(pt_sim *s) { delete s; }
 
 const char *pt_last_error(const pt_sim *s)
 {
     if (!s) return g_create_error.c_str();
     return s->err.c_str();
+}
+
+// ------------------------------------------------------------------ batches
+pt_status pt_batch_create(const pt_params *params, const int *core_seeds, int instances, void *cuda_stream,
+                          pt_batch **out)
+{
+    if (!params || !core_seeds || !out) return fail(nullptr, PT_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (instances < 1 || instances > PT_BATCH_MAX_INSTANCES)
+        return fail(nullptr, PT_ERR_ARG, "instances must be in 1.." + std::to_string(PT_BATCH_MAX_INSTANCES));
+    std::unique_ptr<pt_batch> b(new pt_batch());
+    pt_status st = engine_create(b.get(), params, core_seeds, instances, cuda_stream);
+    if (st != PT_OK) return st;
+    *out = b.release();
+    return PT_OK;
+}
+
+pt_status pt_batch_setup(pt_batch *b)
+{
+    if (!b) return PT_ERR_ARG;
+    return engine_setup(b);
+}
+
+pt_status pt_batch_run(pt_batch *b)
+{
+    if (!b) return PT_ERR_ARG;
+    return engine_run(b);
+}
+
+pt_status pt_batch_step_day(pt_batch *b, int *running)
+{
+    if (!b) return PT_ERR_ARG;
+    return engine_step(b, running);
+}
+
+pt_status pt_batch_reset_epidemic(pt_batch *b)
+{
+    if (!b) return PT_ERR_ARG;
+    if (!b->setup_done) return fail(b, PT_ERR_STATE, "reset before setup");
+    return engine_reset(b);
+}
+
+pt_status pt_batch_size(const pt_batch *b, int *instances, int64_t *persons, int64_t *padded_persons)
+{
+    if (!b) return PT_ERR_ARG;
+    if (instances) *instances = b->K();
+    if (persons) *persons = b->persons;
+    if (padded_persons) *padded_persons = b->setup_done ? b->d.P : 0;
+    return PT_OK;
+}
+
+static bool bad_instance(const pt_batch *b, int k) { return !b || k < 0 || k >= b->K(); }
+
+pt_status pt_batch_counts(const pt_batch *b, int k, int *counts, int *infected, int *days_run)
+{
+    if (bad_instance(b, k)) return PT_ERR_ARG;
+    const Instance &in = b->inst[k];
+    if (counts) std::memcpy(counts, in.counts.data(), (size_t)in.days_run * 16 * sizeof(int));
+    if (infected) std::memcpy(infected, in.infected.data(), (size_t)in.days_run * sizeof(int));
+    if (days_run) *days_run = in.days_run;
+    return PT_OK;
+}
+
+pt_status pt_batch_final_gen_counts(pt_batch *b, int *gen_p, int *gen_s)
+{
+    if (!b || !gen_p || !gen_s) return PT_ERR_ARG;
+    return engine_gen_counts(b, gen_p, gen_s);
+}
+
+pt_status pt_batch_get_info(const pt_batch *b, int k, pt_info *out)
+{
+    if (bad_instance(b, k) || !out) return PT_ERR_ARG;
+    return engine_info(b, k, out);
+}
+
+pt_status pt_batch_get_person_state(pt_batch *b, int k, uint8_t *status_p, uint8_t *status_s, uint8_t *day_p,
+                                    uint8_t *day_s, uint8_t *gen_p, uint8_t *gen_s, uint8_t *age)
+{
+    if (bad_instance(b, k)) return PT_ERR_ARG;
+    return engine_person_state(b, k, status_p, status_s, day_p, day_s, gen_p, gen_s, age);
+}
+
+pt_status pt_batch_get_population(pt_batch *b, int k, int32_t *household, int32_t *household_offset,
+                                  int32_t *workplace, int32_t *workplace_people, int32_t *workplace_offset)
+{
+    if (bad_instance(b, k)) return PT_ERR_ARG;
+    return engine_population(b, k, household, household_offset, workplace, workplace_people, workplace_offset);
+}
+
+pt_status pt_batch_set_timing(pt_batch *b, int enabled)
+{
+    if (!b) return PT_ERR_ARG;
+    return engine_set_timing(b, enabled);
+}
+
+pt_status pt_batch_get_stage_ms(pt_batch *b, float ms[16], int days[2])
+{
+    if (!b || !ms) return PT_ERR_ARG;
+    return engine_stage_ms(b, ms, days);
+}
+
+pt_status pt_batch_transfer_bytes(const pt_batch *b, uint64_t *h2d, uint64_t *d2h)
+{
+    if (!b) return PT_ERR_ARG;
+    if (h2d) *h2d = b->h2d_bytes;
+    if (d2h) *d2h = b->d2h_bytes;
+    return PT_OK;
+}
+
+void pt_batch_destroy(pt_batch *b) { delete b; }
+
+const char *pt_batch_last_error(const pt_batch *b)
+{
+    if (!b) return g_create_error.c_str();
+    return b->err.c_str();
 }
 
 }  // extern "C"
