@@ -216,6 +216,106 @@ def run_reference(args, world, rank):
     return 0
 
 
+def run_batched(args, pt, torch, stream, local):
+    """The batched workload (256 uneven instances x 100 days, one batch) and the same
+    instances run one after another through the plain path, both timed with CUDA
+    events on the same stream after warm-up."""
+    from pandemicthrust_gb300 import scenarios
+    params, seeds = scenarios.batched_workload(count=args.batch_instances)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    b = pt.PandemicBatch(params, seeds, stream=sp)
+    b.setup()
+    K, persons, padded = b.size()
+    sizes = [b.info(k)["number_people"] for k in range(K)]
+    for _ in range(args.batch_warmup):
+        b.reset_epidemic()
+        b.run()
+    sampler = ClockSampler(local)
+    torch.cuda.synchronize()
+    sampler.start()
+    launches0 = pt.launch_count()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    person_days = 0
+    for _ in range(args.batch_steps):
+        b.reset_epidemic()
+        b.run()
+        person_days += sum(n * int(d) for n, d in zip(sizes, b.days_run()))
+    t1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    launches = pt.launch_count() - launches0
+    ms = t0.elapsed_time(t1)
+    value = person_days / (ms / 1000.0)
+    days = b.days_run()
+    # stage breakdown: one more run with per-stage CUDA events (outside the timed region)
+    b.set_timing(True)
+    b.reset_epidemic()
+    b.run()
+    stages, _ = b.stage_ms()
+    b.set_timing(False)
+    tot = {n: stages["weekday"][n] + stages["weekend"][n] for n in pt.PandemicSim.STAGES}
+    run_ms = sum(tot.values())
+    breakdown = {n: {"ms": round(v, 2), "share": round(v / run_ms, 4) if run_ms else None} for n, v in tot.items()}
+    infected_days = 0
+    for k in range(K):
+        infected_days += int(b.counts(k)[1].sum())
+    b.close()
+    # e2e: create + setup + run + generation counts + destroy through the C ABI
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b2 = pt.PandemicBatch(params, seeds, stream=sp)
+    b2.setup()
+    b2.run()
+    b2.final_gen_counts()
+    e2e_pd = sum(n * int(d) for n, d in zip(sizes, b2.days_run()))
+    h2d, d2h = b2.transfer_bytes()
+    b2.close()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    # the same instances run one after another through the plain path (each after one
+    # warm-up run, so its day loop is already a captured graph)
+    plain_ms = 0.0
+    plain_pd = 0
+    for p, sd in zip(params, seeds):
+        sim = pt.PandemicSim(p, sd, stream=sp)
+        sim.setupSim()
+        sim.runToCompletion()
+        sim.reset_epidemic()
+        torch.cuda.synchronize()
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        _, inf = sim.runToCompletion()
+        a1.record(stream)
+        torch.cuda.synchronize()
+        plain_ms += a0.elapsed_time(a1)
+        plain_pd += sim.info()["number_people"] * len(inf)
+        sim.close()
+    plain_value = plain_pd / (plain_ms / 1000.0)
+    return {
+        "workload": "batched_%d_instances_100_days" % K, "instances": K, "persons": persons,
+        "padded_persons": padded, "value": value, "unit": UNIT, "steps": args.batch_steps,
+        "warmup": args.batch_warmup, "ms_per_step": ms / args.batch_steps,
+        "days_run": {"min": int(min(days)), "max": int(max(days)), "mean": float(sum(days)) / K},
+        "gpu_launches": launches,
+        "stages": breakdown,
+        "infected_fraction_mean": infected_days / max(float(sum(n * int(d) for n, d in zip(sizes, days))), 1.0),
+        "e2e": {"value": e2e_pd / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "plain_sequential": {"value": plain_value, "unit": UNIT, "ms": plain_ms,
+                             "note": "each instance alone through the plain path, device time of its run"},
+        "speedup_vs_plain_sequential": value / plain_value,
+        "config": "persons log-uniform in [2e5, 4e6], R per strain uniform in [1.1, 2.0], 10 + 10 seeds, "
+                  "seed 1000 + k, inputs larger than L2",
+        "clocks": clocks,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -225,6 +325,11 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-days", type=int, default=7)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch-instances", type=int, default=256,
+                    help="instances of the batched workload (0: skip it)")
+    ap.add_argument("--batch-steps", type=int, default=3)
+    ap.add_argument("--batch-warmup", type=int, default=3)
+    ap.add_argument("--only-batched", action="store_true", help="run the batched workload alone")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="population scale (profiling captures only; the bench line is for 1.0)")
     args = ap.parse_args()
@@ -240,6 +345,10 @@ def main():
     import pandemicthrust_gb300 as pt
     pt.build()
     stream = torch.cuda.Stream()
+    if args.only_batched:
+        if rank == 0:
+            print(json.dumps(run_batched(args, pt, torch, stream, local)))
+        return 0
     seed = SEED + rank
     params = dict(PARAMS)
     params["people_scaling"] = PARAMS["people_scaling"] * args.scale
@@ -350,6 +459,10 @@ def main():
     else:
         sim.close()
 
+    batched = None
+    if args.batch_instances > 0 and world == 1:
+        batched = run_batched(args, pt, torch, stream, local)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -378,6 +491,7 @@ def main():
             "buckets_materialised_fraction": round(mat_frac, 4),
             "cpu_baseline": cpu,
             "clocks": clocks,
+            "batched": batched,
         }
         print(json.dumps(line))
     if world > 1:

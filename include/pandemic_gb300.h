@@ -131,7 +131,8 @@ pt_status pt_get_population(pt_sim *sim, int32_t *household, int32_t *household_
  * offsets (2L+1 / 10L+1), in the reference's layout (key = hour * L + location).
  * entries and buckets receive the sizes.  By default a day materialises only the
  * buckets that its infected persons visit (the only ones the contact draws read), so
- * the person table is complete only after pt_set_full_tables(sim, 1). */
+ * the person table and the offsets of the other buckets are complete only after
+ * pt_set_full_tables(sim, 1). */
 pt_status pt_get_day_tables(pt_sim *sim, int32_t *infected, int32_t *keys, int32_t *people,
                             int32_t *offsets, int *entries, int *buckets);
 

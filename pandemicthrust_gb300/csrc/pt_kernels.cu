@@ -181,15 +181,21 @@ cudaError_t launch_scan_exclusive(const int32_t *in, int32_t *out, int n, int cl
 
 // Exclusive scan of each pass's 256-bin digit histogram -> digit bases; clears the
 // histograms for the next sort.
-__global__ void k_digit_bases(int *digit_hist, int *digit_base, int passes, const int *skip)
+// With stripes > 1 the histograms are split over `stripes` copies of 4 x 256 bins
+// (producers spread their updates over the copies); the copies are summed.
+__global__ void k_digit_bases(int *digit_hist, int *digit_base, int passes, int stripes, const int *skip)
 {
     if (skip && *(volatile const int *)skip) return;
     for (int p = 0; p < passes; p++) {
-        int v = digit_hist[p * 256 + threadIdx.x];
+        int v = 0;
+        for (int st = 0; st < stripes; st++) {
+            int *h = &digit_hist[(st * kMaxRadixPasses + p) * 256 + threadIdx.x];
+            v += *h;
+            *h = 0;
+        }
         int total;
         int excl = block_exclusive_scan<256, int>(v, total);
         digit_base[p * 256 + threadIdx.x] = excl;
-        digit_hist[p * 256 + threadIdx.x] = 0;
     }
 }
 
@@ -486,7 +492,7 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
             const uint32_t k = s_key[i];
             const unsigned d = (k >> shift) & 255u;
             const int pos = s_base[d] + (i - s_toff[d]);
-            if (MODE == kRadixFirst || MODE == kRadixMiddle) keys_out[pos] = k;
+            if (MODE == kRadixFirst || MODE == kRadixMiddle || keys_out) keys_out[pos] = k;
             vals_out[pos] = s_val[i];
         }
         __syncthreads();
@@ -524,6 +530,8 @@ cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
     for (int p = 0; p < P; p++) {
         cudaError_t e;
         uint32_t *kout = (p & 1) ? r.k1 : r.k0;
+        // the last pass writes keys only when asked to (RadixArgs::keep_keys)
+        if (p == P - 1 && !r.keep_keys) kout = nullptr;
         uint32_t *vout = (p == P - 1) ? r.out : ((p & 1) ? r.v1 : r.v0);
         const int *db = r.digit_base + 256 * p;
         const int shift = 8 * p;
@@ -564,7 +572,7 @@ cudaError_t launch_bucket_table(const RadixArgs &r, int32_t *counts, bool count_
     cudaError_t e = launch_scan_exclusive(counts, offset, r.buckets, 1, tiles, lb_ctl, r.error, r.skip, P,
                                           digit_hist, s, nullptr, nullptr);
     if (e != cudaSuccess) return e;
-    k_digit_bases<<<1, 256, 0, s>>>(digit_hist, (int *)r.digit_base, P, r.skip);
+    k_digit_bases<<<1, 256, 0, s>>>(digit_hist, (int *)r.digit_base, P, 1, r.skip);
     count_launch();
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -668,66 +676,97 @@ __device__ __forceinline__ uint32_t recover_word(uint32_t st, int d2r, bool &cha
 
 // End of the sweep, run by the last block to finish: each running instance's day
 // bookkeeping (runToCompletion, PandemicSim.cu:891-937: the statistics row, the stop
-// on zero infected, the counter offsets E0 / R0 of the schedule and the contacts),
-// and the start of each instance's run of the infected list.
+// on zero infected, the counter offsets E0 / R0 of the schedule and the contacts).
+// An instance's infected are the positions [start, list_end) of today's list,
+// recorded by its first and last tiles.
 __device__ void sweep_day_end(const InstConst *ic, InstState *is, int K, Scalars *sc, int day)
 {
     const bool weekend = (day % 7) >= 5;  // PandemicSim.h:283-284
-    int carry = 0;
-    for (int b = 0; b < K; b += kSweepThreads) {
-        const int k = b + (int)threadIdx.x;
-        int I = 0;
-        if (k < K) {
-            InstState &s = is[k];
-            const int counted = atomicExch(&s.tile_infected, 0);
-            if (instance_running(ic[k], s, day)) {
-                I = counted;
-                s.infected = I;
-                s.infected_per_day[day] = I;
-                s.day = day;
-                s.days_run = day + 1;
-                if (I == 0) {
-                    s.done = 1;
-                } else {
-                    const unsigned long long N = (unsigned long long)ic[k].c.N;
-                    const unsigned long long E0 = s.rand_offset;
-                    const unsigned long long R0 = E0 + (weekend ? 2ull * N : N / 2ull);
-                    s.errand_offset = E0;
-                    s.infect_offset = R0;
-                    s.rand_offset = R0 + 6ull * (unsigned long long)I;
-                }
-            } else {
-                s.infected = 0;
-            }
+    for (int k = threadIdx.x; k < K; k += kSweepThreads) {
+        InstState &s = is[k];
+        if (!instance_running(ic[k], s, day)) {
+            s.infected = 0;
+            continue;
         }
-        int total;
-        const int excl = block_exclusive_scan<kSweepThreads, int>(I, total);
-        if (k < K) is[k].start = carry + excl;
-        carry += total;
+        const int I = *(volatile int *)&s.list_end - *(volatile int *)&s.start;
+        s.infected = I;
+        s.infected_per_day[day] = I;
+        s.day = day;
+        s.days_run = day + 1;
+        if (I == 0) {
+            s.done = 1;
+        } else {
+            const unsigned long long N = (unsigned long long)ic[k].c.N;
+            const unsigned long long E0 = s.rand_offset;
+            const unsigned long long R0 = E0 + (weekend ? 2ull * N : N / 2ull);
+            s.errand_offset = E0;
+            s.infect_offset = R0;
+            s.rand_offset = R0 + 6ull * (unsigned long long)I;
+        }
     }
     if (threadIdx.x == 0) {
-        sc->infected = carry;
         sc->day = day;
         sc->new_count = 0;
-        if (carry == 0) sc->done = 1;
+        if (*(volatile int *)&sc->infected == 0) sc->done = 1;
     }
+}
+
+// A day kernel's person tile: its look-back ticket and the instance it belongs to.
+// Thread 0 takes the ticket; with a single instance the instance record is read in
+// parallel with the ticket's round trip instead of after it.
+struct TileInfo {
+    int tile;
+    unsigned epoch;
+    int inst, pbase, pend, first_person_after;  // first_person_after: pbase + N, or the tile start if not running
+};
+
+__device__ __forceinline__ void tile_begin(const LookBack &lb, const InstConst *ic, const InstState *is,
+                                           const int32_t *tile_inst, int K, int day, TileInfo &out)
+{
+    __shared__ TileInfo s_t;
+    if (threadIdx.x == 0) {
+        TileInfo t;
+        int N = 0, running = 0;
+        if (K == 1) {
+            t.inst = 0;
+            t.pbase = ic[0].pbase;
+            t.pend = ic[0].pend;
+            N = ic[0].c.N;
+            running = instance_running(ic[0], is[0], day);
+        }
+        t.tile = atomicAdd(&lb.ctl[0], 1);
+        t.epoch = (unsigned)(*(volatile int *)&lb.ctl[2]) & 0x3FFFFFFFu;
+        if (K != 1) {
+            const int k = tile_inst[t.tile];
+            t.inst = k;
+            t.pbase = ic[k].pbase;
+            t.pend = ic[k].pend;
+            N = ic[k].c.N;
+            running = instance_running(ic[k], is[k], day);
+        }
+        t.first_person_after = running ? t.pbase + N : t.tile * kPersonTile;
+        s_t = t;
+    }
+    __syncthreads();
+    out = s_t;
 }
 
 // kernel_countInfectedStatusAndRecover (PandemicSim.cu:2097-2192) and the copy_if
 // of the infected (:2207-2224) in one pass: recover, count the 16 status bins of the
 // instance, and write the ascending infected list by a decoupled look-back.
-__global__ void __launch_bounds__(kSweepThreads) k_sweep(const InstConst *ic, InstState *is, const int32_t *tile_inst,
+__global__ void __launch_bounds__(kSweepThreads, 8) k_sweep(const InstConst *ic, InstState *is, const int32_t *tile_inst,
                                                          int K, uint32_t *state, int32_t *infected,
                                                          int32_t *infected_inst, Scalars *sc, LookBack lb, int day)
 {
     if (*(volatile int *)&sc->done) return;
-    int tile;
-    unsigned epoch;
-    lookback_begin(lb, tile, epoch);
-    const int k = tile_inst[tile];
+    TileInfo ti;
+    tile_begin(lb, ic, is, tile_inst, K, day, ti);
+    const int tile = ti.tile;
+    const unsigned epoch = ti.epoch;
+    const int k = ti.inst;
     const long long tile_base = (long long)tile * kSweepTile;
     // end of the tile's persons: none when the instance no longer runs
-    const long long N = instance_running(ic[k], is[k], day) ? (long long)ic[k].pbase + ic[k].c.N : tile_base;
+    const long long N = ti.first_person_after;
     const int d2r = day - 10;
     // packed per-thread status bins: 16-bit fields, bins 0-3 / 4-7 per strain
     unsigned long long bp_lo = 0, bp_hi = 0, bs_lo = 0, bs_hi = 0;
@@ -835,12 +874,20 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(const InstConst *ic, In
         }
     }
     if (threadIdx.x < 16 && s_bins[threadIdx.x]) atomicAdd(&is[k].counts[day][threadIdx.x], s_bins[threadIdx.x]);
-    if (threadIdx.x == 0 && tile_total) atomicAdd(&is[k].tile_infected, (int)tile_total);
-    // the last block to finish closes the day of every instance
-    __threadfence();
+    if (threadIdx.x == 0) {
+        // the instance's run of the infected list, and the list's length
+        if (tile_base == ti.pbase) is[k].start = (int)prefix;
+        if (tile_base + kSweepTile == ti.pend) is[k].list_end = (int)(prefix + tile_total);
+        if (tile == (int)gridDim.x - 1) sc->infected = (int)(prefix + tile_total);
+    }
+    // the last block to finish closes the day of every instance (the barrier, then
+    // one release fence, orders the block's updates before its finish count)
     __syncthreads();
     __shared__ int s_last;
-    if (threadIdx.x == 0) s_last = atomicAdd(&lb.ctl[1], 1) == (int)gridDim.x - 1;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&lb.ctl[1], 1) == (int)gridDim.x - 1;
+    }
     __syncthreads();
     if (!s_last) return;
     __threadfence();
@@ -890,6 +937,40 @@ __device__ __forceinline__ void weekday_pair_keys(const SimConst &c, const uint3
 
 __device__ __forceinline__ bool is_marked(const uint32_t *mark, int b) { return (mark[b >> 5] >> (b & 31)) & 1u; }
 
+// Fire-and-forget global updates (PTX red): the thread does not wait for the result.
+__device__ __forceinline__ void red_add(int *p, int v)
+{
+    asm volatile("red.relaxed.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void red_or(uint32_t *p, uint32_t v)
+{
+    asm volatile("red.relaxed.gpu.global.or.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void mark_bucket(uint32_t *mark, int b) { red_or(&mark[b >> 5], 1u << (b & 31)); }
+
+// Adds this lane's key b (when `on`) to the block's digit histograms of the radix
+// passes.  Called by all 32 lanes.  The lower digits are spread out and each lane
+// adds its own; the top digit of a tile's keys is often the same across the warp,
+// and then one lane adds the count.
+__device__ __forceinline__ void digit_count(int (*s_dh)[256], int passes, bool on, uint32_t b)
+{
+    const unsigned act = __ballot_sync(0xffffffffu, on);
+    if (!act) return;
+    if (on)
+        for (int p = 0; p < passes - 1; p++) atomicAdd(&s_dh[p][(b >> (8 * p)) & 255u], 1);
+    const int top = passes - 1;
+    const uint32_t d = (b >> (8 * top)) & 255u;
+    const int leader = __ffs(act) - 1;
+    const uint32_t d0 = __shfl_sync(0xffffffffu, d, leader);
+    if (__all_sync(0xffffffffu, !on || d == d0)) {
+        if ((int)(threadIdx.x & 31) == leader) atomicAdd(&s_dh[top][d0], __popc(act));
+    } else if (on) {
+        atomicAdd(&s_dh[top][d], 1);
+    }
+}
+
 // Marks the errand buckets today's contact draws will read: the only buckets that
 // must be materialised.  Destinations are regenerated from the schedule counter, as
 // the reference's device_recalc_* functions do (PandemicSim.cu:3667-3705,
@@ -920,8 +1001,7 @@ __global__ void k_mark_buckets(const InstConst *ic, const InstState *is, const u
             const int prof = (int)(w[3] % 6u);
 #pragma unroll
             for (int j = 0; j < 2; j++) {
-                const int b = ik.bbase[1] + d[c_weekend_assign[prof][j]];
-                atomicOr(&mark[b >> 5], 1u << (b & 31));
+                mark_bucket(mark, ik.bbase[1] + d[c_weekend_assign[prof][j]]);
             }
         } else {
             const int lo = c.type_offset[8], R = c.L - lo;
@@ -934,8 +1014,8 @@ __global__ void k_mark_buckets(const InstConst *ic, const InstState *is, const u
             k1 += ik.bbase[0];
             k2 += ik.bbase[0];
             const int prof = adult ? (int)((w[slot] ^ w[slot + 1]) % 3u) : 3;
-            if (c_weekday_assign[prof][0] > 0) atomicOr(&mark[k1 >> 5], 1u << (k1 & 31));
-            if (c_weekday_assign[prof][1] > 0) atomicOr(&mark[k2 >> 5], 1u << (k2 & 31));
+            if (c_weekday_assign[prof][0] > 0) mark_bucket(mark, k1);
+            if (c_weekday_assign[prof][1] > 0) mark_bucket(mark, k2);
         }
     }
 }
@@ -943,42 +1023,51 @@ __global__ void k_mark_buckets(const InstConst *ic, const InstState *is, const u
 // Schedule kernel, one person tile per block.  Warps own 512 consecutive persons and
 // walk them in rounds (weekday: 64 persons a round, a pair per lane, one Threefry
 // block per pair; weekend: 32 persons a round, one per lane), so key writes are
-// coalesced.  The kernel writes every person's keys, counts the entries of marked
-// buckets and appends those entries as (key, person) in ascending person order
-// (warp scans + block scan + decoupled look-back): the order the radix sort needs
-// for stability.  Per-round marked counts of a lane are packed in one register
-// between the two phases.  The instance's constants are staged in shared memory.
+// coalesced.  The kernel writes every person's keys, accumulates the radix digit
+// histograms of the entries of marked buckets in shared memory, and appends those
+// entries as (key, person) in ascending person order (warp scans + block scan +
+// decoupled look-back): the order the radix sort needs for stability.  Per-round
+// marked counts of a lane are packed in one register between the two phases.  The
+// instance's constants are staged in shared memory.
 constexpr int kSchedThreads = 256, kSchedTile = kPersonTile, kSchedWarpPersons = 512;
 
 template <bool WEEKEND>
-__global__ void __launch_bounds__(kSchedThreads) k_sched(const InstConst *ic, const InstState *is,
-                                                         const int32_t *tile_inst, const uint8_t *age,
-                                                         const uint32_t *mark, int32_t *keys, int32_t *count,
-                                                         uint32_t *ckeys, uint32_t *cvals, Scalars *sc, LookBack lb,
-                                                         int day)
+__global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic, const InstState *is,
+                                                         const int32_t *tile_inst, int K, const uint8_t *age,
+                                                         const uint32_t *mark, int32_t *keys, int *digit_hist,
+                                                         int passes, uint32_t *ckeys, uint32_t *cvals, Scalars *sc,
+                                                         LookBack lb, int day)
 {
     if (*(volatile int *)&sc->done) return;
-    int tile;
-    unsigned epoch;
-    lookback_begin(lb, tile, epoch);
-    const int inst = tile_inst[tile];
+    __shared__ int s_dh[kMaxRadixPasses][256];   // digit histograms of the marked entries
+    for (int i = threadIdx.x; i < kMaxRadixPasses * 256; i += kSchedThreads) (&s_dh[0][0])[i] = 0;
     __shared__ SimConst s_c;
-    {
-        const int *src = reinterpret_cast<const int *>(&ic[inst].c);
-        int *dst = reinterpret_cast<int *>(&s_c);
-        for (int i = threadIdx.x; i < (int)(sizeof(SimConst) / 4); i += kSchedThreads) dst[i] = src[i];
-    }
+    const int csz = (int)(sizeof(SimConst) / 4);
+    if (K == 1)  // the only instance: copy its constants while thread 0 takes the ticket
+        for (int i = threadIdx.x; i < csz; i += kSchedThreads)
+            reinterpret_cast<int *>(&s_c)[i] = reinterpret_cast<const int *>(&ic[0].c)[i];
+    TileInfo ti;
+    tile_begin(lb, ic, is, tile_inst, K, day, ti);
+    const int tile = ti.tile;
+    const unsigned epoch = ti.epoch;
+    const int inst = ti.inst;
+    if (K != 1)
+        for (int i = threadIdx.x; i < csz; i += kSchedThreads)
+            reinterpret_cast<int *>(&s_c)[i] = reinterpret_cast<const int *>(&ic[inst].c)[i];
+    const int pbase = ti.pbase;
+    const int N = ti.first_person_after - pbase;   // persons to schedule (0 when not running)
+    const int tbase = tile * kSchedTile - pbase;   // the tile's first person, instance numbering
+    const int valid = N - tbase < kSchedTile ? (N - tbase > 0 ? N - tbase : 0) : kSchedTile;
+    int32_t *kk = keys + ic[inst].kbase;   // the instance's key slots
+    const int NK = ic[inst].c.N;           // their layout: weekday hour 0 at [0, N), hour 1 at [N, 2N)
+    const uint8_t *tage = age + pbase + tbase;
     __syncthreads();
     const SimConst &c = s_c;
     const TfKey key = make_key(c);
-    const int pbase = ic[inst].pbase;
     const int bb = ic[inst].bbase[WEEKEND ? 1 : 0];
-    int32_t *kk = keys + ic[inst].kbase;                                   // the instance's key slots
-    const int NK = c.N;                                                    // key layout
-    const int N = instance_running(ic[inst], is[inst], day) ? c.N : 0;    // persons to schedule
     const unsigned long long E0 = is[inst].errand_offset;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int wbase = tile * kSchedTile - pbase + warp * kSchedWarpPersons;  // the instance's person number
+    const int wl = warp * kSchedWarpPersons;      // the warp's first person, tile numbering
     constexpr int kRounds = WEEKEND ? 16 : 8;
     constexpr int kBits = WEEKEND ? 2 : 3;  // marked entries per lane and round: <= 3 / <= 4
     uint32_t cpack = 0;
@@ -988,21 +1077,22 @@ __global__ void __launch_bounds__(kSchedThreads) k_sched(const InstConst *ic, co
         const int lo = c.type_offset[9], R = c.L - lo;
 #pragma unroll 1
         for (int j = 0; j < kRounds; j++) {
-            const int p = wbase + 32 * j + lane;
-            int cnt = 0;
-            if (p < N) {
+            const int i = wl + 32 * j + lane;
+            uint32_t kb[3] = {0u, 0u, 0u};
+            bool mk[3] = {false, false, false};
+            if (i < valid) {
                 int d[3];
-                weekend_errands(c, key, E0 + 2ull * (unsigned long long)p, lo, R, d);
+                weekend_errands(c, key, E0 + 2ull * (unsigned long long)(tbase + i), lo, R, d);
 #pragma unroll
                 for (int k = 0; k < 3; k++) {
-                    const int b = bb + d[k];
-                    kk[3 * (size_t)p + k] = b;
-                    if (is_marked(mark, b)) {
-                        atomicAdd(&count[b], 1);
-                        cnt++;
-                    }
+                    kb[k] = (uint32_t)(bb + d[k]);
+                    kk[3 * (size_t)(tbase + i) + k] = (int32_t)kb[k];
+                    mk[k] = is_marked(mark, (int)kb[k]);
                 }
             }
+            const int cnt = (int)mk[0] + (int)mk[1] + (int)mk[2];
+#pragma unroll
+            for (int k = 0; k < 3; k++) digit_count(s_dh, passes, mk[k], kb[k]);
             cpack |= (uint32_t)cnt << (kBits * j);
             mine += cnt;
         }
@@ -1010,32 +1100,29 @@ __global__ void __launch_bounds__(kSchedThreads) k_sched(const InstConst *ic, co
         const int lo = c.type_offset[8], R = c.L - lo;
 #pragma unroll 1
         for (int j = 0; j < kRounds; j++) {
-            const int p = wbase + 64 * j + 2 * lane;  // even: counter E0 + p/2 covers p, p+1
-            int cnt = 0;
-            if (p < N) {
+            const int i = wl + 64 * j + 2 * lane;  // even: counter E0 + p/2 covers p, p+1
+            uint32_t kb[4] = {0u, 0u, 0u, 0u};
+            bool mk[4] = {false, false, false, false};
+            if (i < valid) {
                 uint32_t w[4];
-                tf2x64(key, E0 + (uint64_t)(p / 2), w);
+                tf2x64(key, E0 + (uint64_t)((tbase + i) / 2), w);
 #pragma unroll
                 for (int k = 0; k < 2; k++) {
-                    const int q = p + k;
-                    if (q < N) {
+                    if (i + k < valid) {
                         int k1, k2;
-                        weekday_pair_keys(c, w, k, age[pbase + q] == 5, lo, R, k1, k2);
-                        k1 += bb;
-                        k2 += bb;
-                        kk[q] = k1;
-                        kk[(size_t)NK + q] = k2;
-                        if (is_marked(mark, k1)) {
-                            atomicAdd(&count[k1], 1);
-                            cnt++;
-                        }
-                        if (is_marked(mark, k2)) {
-                            atomicAdd(&count[k2], 1);
-                            cnt++;
-                        }
+                        weekday_pair_keys(c, w, k, tage[i + k] == 5, lo, R, k1, k2);
+                        kb[2 * k] = (uint32_t)(k1 + bb);
+                        kb[2 * k + 1] = (uint32_t)(k2 + bb);
+                        kk[tbase + i + k] = (int32_t)kb[2 * k];
+                        kk[(size_t)NK + tbase + i + k] = (int32_t)kb[2 * k + 1];
+                        mk[2 * k] = is_marked(mark, (int)kb[2 * k]);
+                        mk[2 * k + 1] = is_marked(mark, (int)kb[2 * k + 1]);
                     }
                 }
             }
+            const int cnt = (int)mk[0] + (int)mk[1] + (int)mk[2] + (int)mk[3];
+#pragma unroll
+            for (int k = 0; k < 4; k++) digit_count(s_dh, passes, mk[k], kb[k]);
             cpack |= (uint32_t)cnt << (kBits * j);
             mine += cnt;
         }
@@ -1058,13 +1145,24 @@ __global__ void __launch_bounds__(kSchedThreads) k_sched(const InstConst *ic, co
                 s_wbase[w] = run;
                 run += s_wtot[w];
             }
-            if (tile == (int)gridDim.x - 1) sc->marked_entries = run;
+            if (tile == (int)gridDim.x - 1) {
+                sc->marked_entries = run;
+                sc->materialised_sum += (unsigned long long)run;
+            }
         }
     }
     __syncthreads();
+    {
+        int *h = digit_hist + (size_t)(blockIdx.x % kDigitStripes) * kMaxRadixPasses * 256;
+        for (int p = 0; p < passes; p++) {
+            const int v = s_dh[p][threadIdx.x];
+            if (v) red_add(&h[p * 256 + threadIdx.x], v);
+        }
+    }
     // append the marked entries, rounds in order, lanes in order within a round
     int run = s_wbase[warp];
     const uint32_t cmask = (1u << kBits) - 1u;
+    const int gbase = pbase + tbase;   // global id of the tile's first person
 #pragma unroll 1
     for (int j = 0; j < kRounds; j++) {
         const int cnt = (int)((cpack >> (kBits * j)) & cmask);
@@ -1073,28 +1171,27 @@ __global__ void __launch_bounds__(kSchedThreads) k_sched(const InstConst *ic, co
         int pos = run + incl - cnt;
         if (cnt > 0) {
             if (WEEKEND) {
-                const int p = wbase + 32 * j + lane;
+                const int i = wl + 32 * j + lane;
 #pragma unroll
                 for (int k = 0; k < 3; k++) {
-                    const int b = kk[3 * (size_t)p + k];
-                    if (is_marked(mark, b)) {
-                        ckeys[pos] = (uint32_t)b;
-                        cvals[pos] = (uint32_t)(pbase + p);
+                    const uint32_t b = (uint32_t)kk[3 * (size_t)(tbase + i) + k];
+                    if (is_marked(mark, (int)b)) {
+                        ckeys[pos] = b;
+                        cvals[pos] = (uint32_t)(gbase + i);
                         pos++;
                     }
                 }
             } else {
-                const int p = wbase + 64 * j + 2 * lane;
+                const int i = wl + 64 * j + 2 * lane;
 #pragma unroll
                 for (int k = 0; k < 2; k++) {
-                    const int q = p + k;
-                    if (q < N) {
+                    if (i + k < valid) {
 #pragma unroll
                         for (int h = 0; h < 2; h++) {
-                            const int b = kk[(size_t)h * NK + q];
-                            if (is_marked(mark, b)) {
-                                ckeys[pos] = (uint32_t)b;
-                                cvals[pos] = (uint32_t)(pbase + q);
+                            const uint32_t b = (uint32_t)kk[(size_t)h * NK + tbase + i + k];
+                            if (is_marked(mark, (int)b)) {
+                                ckeys[pos] = b;
+                                cvals[pos] = (uint32_t)(gbase + i + k);
                                 pos++;
                             }
                         }
@@ -1127,12 +1224,13 @@ cudaError_t launch_schedule(const DevArrays &d, bool weekend, int day, bool full
     }
     const int blocks = d.P / kSchedTile;
     const LookBack lb = make_lb(d);
+    const int passes = radix_passes(B);
     if (weekend)
-        k_sched<true><<<blocks, kSchedThreads, 0, s>>>(d.ic, d.is, d.tile_inst, d.age, d.mark, d.keys, d.bkt_count,
-                                                       d.rk1, d.rv1, d.sc, lb, day);
+        k_sched<true><<<blocks, kSchedThreads, 0, s>>>(
+            d.ic, d.is, d.tile_inst, d.K, d.age, d.mark, d.keys, d.digit_hist, passes, d.rk1, d.rv1, d.sc, lb, day);
     else
-        k_sched<false><<<blocks, kSchedThreads, 0, s>>>(d.ic, d.is, d.tile_inst, d.age, d.mark, d.keys, d.bkt_count,
-                                                        d.rk1, d.rv1, d.sc, lb, day);
+        k_sched<false><<<blocks, kSchedThreads, 0, s>>>(
+            d.ic, d.is, d.tile_inst, d.K, d.age, d.mark, d.keys, d.digit_hist, passes, d.rk1, d.rv1, d.sc, lb, day);
     count_launch();
     return cudaGetLastError();
 }
@@ -1156,25 +1254,55 @@ static RadixArgs day_radix_args(const DevArrays &d, bool weekend)
     r.ctl = d.radix_ctl;
     r.error = &d.sc->error;
     r.skip = &d.sc->done;
+    r.keep_keys = true;  // the bucket offsets come from the sorted keys
     return r;
 }
 
+// The schedule kernel accumulated the digit histograms of the marked entries; their
+// exclusive scans are the radix passes' digit bases.
 cudaError_t launch_bucket_scan(const DevArrays &d, bool weekend, cudaStream_t s)
 {
-    const int B = d.buckets[weekend ? 1 : 0];
-    const int P = radix_passes(B);
-    cudaError_t e = launch_scan_exclusive(d.bkt_count, d.bkt_offset, B, 1, d.tiles, (int *)(d.tiles + d.tiles_cap),
-                                          &d.sc->error, &d.sc->done, P, d.digit_hist, s, nullptr, nullptr,
-                                          &d.sc->materialised_sum);
-    if (e != cudaSuccess) return e;
-    k_digit_bases<<<1, 256, 0, s>>>(d.digit_hist, d.digit_base, P, &d.sc->done);
+    const int P = radix_passes(d.buckets[weekend ? 1 : 0]);
+    k_digit_bases<<<1, 256, 0, s>>>(d.digit_hist, d.digit_base, P, kDigitStripes, &d.sc->done);
     count_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_bucket_sort(const DevArrays &d, bool weekend, cudaStream_t s)
+// Bucket offsets from the sorted keys of the day's materialised entries: entry i
+// starts bucket keys[i] when that differs from keys[i-1] (thrust::lower_bound in
+// the reference, PandemicSim.cu:1240-1248).  Lazy tables write only the offsets the
+// infection kernels read: the start of each bucket with entries and the end of the
+// bucket before it.  Every bucket an infected person reads holds that person, so it
+// has entries.  Complete tables write every offset, empty buckets included.
+__global__ void k_bucket_offsets(const uint32_t *keys, const int *count_dev, int B, int full, int32_t *offset,
+                                 const int *skip)
 {
-    return launch_radix_sort(day_radix_args(d, weekend), s);
+    if (*(volatile const int *)skip) return;
+    const int E = *count_dev;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= E; i += gridDim.x * blockDim.x) {
+        const int prev = i == 0 ? -1 : (int)keys[i - 1];
+        const int cur = i == E ? B : (int)keys[i];
+        if (prev == cur) continue;
+        if (full) {
+            for (int b = prev + 1; b <= cur; b++) offset[b] = i;
+        } else {
+            offset[prev + 1] = i;
+            offset[cur] = i;
+        }
+    }
+}
+
+cudaError_t launch_bucket_sort(const DevArrays &d, bool weekend, bool full_tables, cudaStream_t s)
+{
+    const RadixArgs r = day_radix_args(d, weekend);
+    cudaError_t e = launch_radix_sort(r, s);
+    if (e != cudaSuccess) return e;
+    const int P = radix_passes(r.buckets);
+    const uint32_t *sorted = ((P - 1) & 1) ? r.k1 : r.k0;  // where the last pass wrote the keys
+    k_bucket_offsets<<<sm_count() * 8, 256, 0, s>>>(sorted, r.count_dev, r.buckets, full_tables ? 1 : 0,
+                                                    d.bkt_offset, r.skip);
+    count_launch();
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------ infection

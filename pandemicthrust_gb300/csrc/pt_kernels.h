@@ -11,6 +11,7 @@ constexpr int kTypes = 14;
 constexpr int kMaxDays = 256;
 
 constexpr int kPersonTile = 4096;  // persons per sweep / schedule tile
+constexpr int kDigitStripes = 16;  // copies of the day's radix digit histograms (spreads the updates)
 
 // Constants of one simulation (setup kernels take them by value; the day kernels
 // read them from the InstConst array).
@@ -32,6 +33,7 @@ struct SimConst {
 struct InstConst {
     SimConst c;            // c.N = the instance's persons
     int pbase;             // first global person (a multiple of kPersonTile)
+    int pend;              // end of its persons and padding (the next instance's pbase)
     int hbase;             // first global household slot; H + 1 slots, the last one
                            // holds the padding persons
     int lbase;             // first global location
@@ -48,10 +50,10 @@ struct InstState {
     unsigned long long infect_offset;   // R0 of the current day's contacts
     int infected;                       // infected count of the current day
     int start;                          // their first position in the batch's infected list
+    int list_end;                       // one past their last position
     int done;                           // set once a day counts zero infected
     int days_run;                       // statistics rows written
     int day;                            // last day run
-    int tile_infected;                  // infected counted so far by today's sweep tiles
     int counts[kMaxDays][16];           // per-day status bins
     int infected_per_day[kMaxDays];
 };
@@ -88,7 +90,7 @@ struct DevArrays {
     uint32_t *rk0, *rv0, *rk1, *rv1;  // 3P each: radix ping-pong keys/values
     unsigned long long *radix_status;  // ceil(3P/4096) x 256 epoch-tagged look-back words
     int *radix_ctl;           // ticket, finished
-    int *digit_hist;          // 4 x 256
+    int *digit_hist;          // kDigitStripes x 4 x 256
     int *digit_base;          // 4 x 256
     uint32_t *mark;           // bitmap over today's buckets: 1 = materialise
     int32_t *infected;        // P ascending infected ids
@@ -136,6 +138,7 @@ struct RadixArgs {
     const uint32_t *mark = nullptr;   // optional bucket filter of the first pass
     const int *count_dev = nullptr;   // entry count after the filter (device)
     uint32_t *k0, *v0, *k1, *v1, *out;
+    bool keep_keys = false;       // the last pass also writes the sorted keys (to k0 / k1 by pass parity)
     const int *digit_base;
     unsigned long long *status;   // look-back words, ceil(E/4096) x 256, epoch-tagged
     int *ctl;                     // ticket, finished, epoch
@@ -159,7 +162,7 @@ cudaError_t launch_seed_infected(const int32_t *seeds, int P, int S, uint32_t *s
 cudaError_t launch_sweep(const DevArrays &d, int day, cudaStream_t s);
 cudaError_t launch_schedule(const DevArrays &d, bool weekend, int day, bool full_tables, cudaStream_t s);
 cudaError_t launch_bucket_scan(const DevArrays &d, bool weekend, cudaStream_t s);
-cudaError_t launch_bucket_sort(const DevArrays &d, bool weekend, cudaStream_t s);
+cudaError_t launch_bucket_sort(const DevArrays &d, bool weekend, bool full_tables, cudaStream_t s);
 cudaError_t launch_infect(const DevArrays &d, bool weekend, int day, cudaStream_t s);
 cudaError_t launch_apply(const DevArrays &d, int day, cudaStream_t s);
 // weekday / weekend buckets of one instance (compact keys hour * R + dest - lo)

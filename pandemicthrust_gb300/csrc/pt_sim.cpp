@@ -287,6 +287,7 @@ static pt_status engine_setup(Engine *s)
         std::memset(&r, 0, sizeof(r));
         r.c = s->inst[k].c;
         r.pbase = pbase[k];
+        r.pend = k + 1 < K ? pbase[k + 1] : (int)P;
         r.hbase = hbase[k];
         r.lbase = lbase[k];
         r.bbase[0] = bbase0[k];
@@ -320,7 +321,7 @@ static pt_status engine_setup(Engine *s)
     bytes += round256(((size_t)Bday + 1) * 4);  // bkt_offset
     bytes += round256((size_t)Bmax * 4);        // bkt_count (also the workplace histogram)
     bytes += round256(radix_tiles * 256 * 8);   // radix look-back words
-    bytes += round256(8 * 4) + 2 * round256(4 * 256 * 4);  // radix ctl, digit hist/base
+    bytes += round256(8 * 4) + round256((size_t)ptk::kDigitStripes * 4 * 256 * 4) + round256(4 * 256 * 4);  // radix ctl, digit hist/base
     bytes += round256(((size_t)Bday / 32 + 1) * 4);        // bucket mark bitmap
     bytes += round256(n * 4) * 2;               // infected, infected_inst
     bytes += round256(2 * n * 8);               // claim
@@ -348,7 +349,7 @@ static pt_status engine_setup(Engine *s)
     d.bkt_count = a.take<int32_t>((size_t)Bmax);
     d.radix_status = a.take<unsigned long long>(radix_tiles * 256);
     d.radix_ctl = a.take<int>(8);
-    d.digit_hist = a.take<int>(4 * 256);
+    d.digit_hist = a.take<int>((size_t)ptk::kDigitStripes * 4 * 256);
     d.digit_base = a.take<int>(4 * 256);
     d.mark = a.take<uint32_t>((size_t)Bday / 32 + 1);
     d.infected = a.take<int32_t>(n);
@@ -371,7 +372,7 @@ static pt_status engine_setup(Engine *s)
     CK(cudaMemsetAsync(d.bkt_count, 0, (size_t)Bmax * 4, s->stream), "memset counts");
     CK(cudaMemsetAsync(d.radix_ctl, 0, 8 * 4, s->stream), "memset radix ctl");
     CK(cudaMemsetAsync(d.radix_status, 0, radix_tiles * 256 * 8, s->stream), "memset radix words");
-    CK(cudaMemsetAsync(d.digit_hist, 0, 4 * 256 * 4, s->stream), "memset digit hist");
+    CK(cudaMemsetAsync(d.digit_hist, 0, (size_t)ptk::kDigitStripes * 4 * 256 * 4, s->stream), "memset digit hist");
 
     // households -> persons, padding persons, then workplaces and schools (setup_assignWorkplaces)
     CK(ptk::launch_generate_households(types, d.hh_offset, (int)HS, d.household, d.age, s->stream), "households");
@@ -470,7 +471,7 @@ static pt_status enqueue_day(Engine *s, int day)
     if (t) cudaEventRecord(stage_event(s, day, 2), st);
     CK(ptk::launch_bucket_scan(d, weekend, st), "bucket scan");
     if (t) cudaEventRecord(stage_event(s, day, 3), st);
-    CK(ptk::launch_bucket_sort(d, weekend, st), "bucket sort");
+    CK(ptk::launch_bucket_sort(d, weekend, s->full_tables, st), "bucket sort");
     if (t) cudaEventRecord(stage_event(s, day, 4), st);
     CK(ptk::launch_infect(d, weekend, day, st), "infect");
     if (t) cudaEventRecord(stage_event(s, day, 5), st);
