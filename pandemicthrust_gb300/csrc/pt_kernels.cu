@@ -362,61 +362,97 @@ __device__ __forceinline__ uint32_t pack_rank(unsigned d, unsigned rank, unsigne
 // device read it from *count_dev.  Persistent blocks take tiles from a ticket in
 // order until the entries run out, so a short input costs no idle blocks.  Look-back
 // words carry the launch epoch (see lb_word), so they need no reset between passes.
+//
+// Segmented sorts (sg.tile_prefix set): segment k's entries lie at
+// [ic[k].kbase, ic[k].kbase + is[k].marked) and are ordered within the segment only,
+// with digit bases of their own (digit_base[(k * passes + pass) * 256 + d]).  The
+// segments' tiles are numbered consecutively (segment k owns tiles
+// [tile_prefix[k], tile_prefix[k + 1])), and the look-back of a segment's first tile
+// starts from zero.  Unsegmented sorts are one segment [0, E).
 template <int MODE>
 __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t *__restrict__ keys_in,
                                                                  const uint32_t *__restrict__ vals_in,
                                                                  uint32_t *__restrict__ keys_out,
                                                                  uint32_t *__restrict__ vals_out, int E_arg,
                                                                  const int *count_dev, const uint32_t *mark,
-                                                                 int shift, int nbits, int N, int person_mode,
-                                                                 const int *__restrict__ digit_base,
-                                                                 unsigned long long *status, int *ctl, int *error,
-                                                                 const int *skip)
+                                                                 int pass, int passes, int nbits, int N,
+                                                                 int person_mode, const int *__restrict__ digit_base,
+                                                                 RadixSegments sg, unsigned long long *status,
+                                                                 int *ctl, int *error, const int *skip)
 {
     if (skip && *(volatile const int *)skip) return;
     __shared__ int s_tile;
+    __shared__ int s_seg[4];      // segment, tile within it, entry base, entry count
     __shared__ unsigned s_epoch;
     __shared__ int s_hist[kRadixWarps][256];
     __shared__ int s_base[256];   // global position of the tile's first entry of each digit
     __shared__ int s_toff[256];   // tile-local position of each digit's first entry
     __shared__ uint32_t s_key[kRadixTile];
     __shared__ uint32_t s_val[kRadixTile];
-    const int E = count_dev ? *(volatile const int *)count_dev : E_arg;
+    const int shift = 8 * pass;
+    int E = 0, tiles;
+    if (sg.tile_prefix) {
+        tiles = *(volatile const int *)&sg.tile_prefix[sg.segments];
+    } else {
+        E = count_dev ? *(volatile const int *)count_dev : E_arg;
+        tiles = (E + kRadixTile - 1) / kRadixTile;
+    }
     // only as many blocks as there are tiles take part (ticket, finish count)
-    const int tiles = (E + kRadixTile - 1) / kRadixTile;
     const int active = tiles < (int)gridDim.x ? tiles : (int)gridDim.x;
     if ((int)blockIdx.x >= active) return;
     if (threadIdx.x == 0) s_epoch = (unsigned)(*(volatile int *)&ctl[2]) & 0x3FFFFFFFu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
     for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(&ctl[0], 1);
+        if (threadIdx.x == 0) {
+            const int t = atomicAdd(&ctl[0], 1);
+            int k = 0, j = t, sbase = 0, scount = E;
+            if (sg.tile_prefix && t < tiles) {
+                // the segment owning tile t: the last k with tile_prefix[k] <= t
+                int lo = 0, hi = sg.segments - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (sg.tile_prefix[mid] <= t) lo = mid;
+                    else hi = mid - 1;
+                }
+                k = lo;
+                j = t - sg.tile_prefix[k];
+                sbase = (int)sg.ic[k].kbase;
+                scount = sg.is[k].marked;
+            }
+            s_tile = t;
+            s_seg[0] = k;
+            s_seg[1] = j;
+            s_seg[2] = sbase;
+            s_seg[3] = scount;
+        }
         __syncthreads();
         const int tile = s_tile;
         const unsigned epoch = s_epoch;
         if (tile >= tiles) break;
+        const int seg = s_seg[0], stile = s_seg[1], sbase = s_seg[2], scount = s_seg[3];
         for (int i = threadIdx.x; i < kRadixWarps * 256; i += kRadixThreads) (&s_hist[0][0])[i] = 0;
         __syncthreads();
-        const int base = tile * kRadixTile + warp * kRadixWarpItems + lane;
-        const bool full = (tile + 1) * kRadixTile <= E;
+        const int base = stile * kRadixTile + warp * kRadixWarpItems + lane;  // index within the segment
+        const bool full = (stile + 1) * kRadixTile <= scount;
         uint32_t key[kRadixItems], val[kRadixItems], info[kRadixItems];
 #pragma unroll
         for (int j = 0; j < kRadixItems; j++) {
             const int i = base + 32 * j;
-            const bool in = full || i < E;
-            key[j] = in ? keys_in[i] : 0u;
+            const bool in = full || i < scount;
+            key[j] = in ? keys_in[sbase + i] : 0u;
             if (MODE == kRadixFirst || MODE == kRadixOnly) {
                 const uint32_t u = (uint32_t)i;
                 val[j] = person_mode == 0 ? u : (person_mode == 1 ? (u < (uint32_t)N ? u : u - (uint32_t)N) : u / 3u);
             } else {
-                val[j] = in ? vals_in[i] : 0u;
+                val[j] = in ? vals_in[sbase + i] : 0u;
             }
         }
         // phase A: rank within the warp round, per-warp digit counts
 #pragma unroll
         for (int j = 0; j < kRadixItems; j++) {
             const int i = base + 32 * j;
-            bool ok = full || i < E;
+            bool ok = full || i < scount;
             if ((MODE == kRadixFirst || MODE == kRadixOnly) && mark && ok)
                 ok = (mark[key[j] >> 5] >> (key[j] & 31u)) & 1u;
             const unsigned d = (key[j] >> shift) & 255u;
@@ -438,8 +474,8 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
             }
             volatile unsigned long long *st = status;
             int excl = 0;
-            if (tile == 0) {
-                st[d] = lb_word(epoch, 2, (unsigned)run);
+            if (stile == 0) {
+                st[(size_t)tile * 256 + d] = lb_word(epoch, 2, (unsigned)run);
             } else {
                 st[(size_t)tile * 256 + d] = lb_word(epoch, 1, (unsigned)run);
                 int t = tile - 1;
@@ -461,7 +497,7 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
                 }
                 st[(size_t)tile * 256 + d] = lb_word(epoch, 2, (unsigned)(excl + run));
             }
-            s_base[d] = digit_base[d] + excl;
+            s_base[d] = sbase + digit_base[((size_t)seg * passes + pass) * 256 + d] + excl;
             // tile-local start of digit d (entries of the tile ordered by digit)
             int tile_total;
             const int toff = block_exclusive_scan<kRadixThreads, int>(run, tile_total);
@@ -533,14 +569,13 @@ cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
         // the last pass writes keys only when asked to (RadixArgs::keep_keys)
         if (p == P - 1 && !r.keep_keys) kout = nullptr;
         uint32_t *vout = (p == P - 1) ? r.out : ((p & 1) ? r.v1 : r.v0);
-        const int *db = r.digit_base + 256 * p;
-        const int shift = 8 * p;
-        const int nbits = std::max(1, std::min(8, bits - shift));
+        const int nbits = std::max(1, std::min(8, bits - 8 * p));
         // the first pass of an implicit-value sort reads all E entries (and may
         // filter); every other pass reads the count on the device, if any
         const int *cnt = (p == 0 && implicit) ? nullptr : r.count_dev;
         const uint32_t *mk = (p == 0) ? r.mark : nullptr;
-#define PT_RADIX_ARGS kin, vin, kout, vout, r.E, cnt, mk, shift, nbits, r.N, r.person_mode, db, r.status, r.ctl, r.error, r.skip
+#define PT_RADIX_ARGS kin, vin, kout, vout, r.E, cnt, mk, p, P, nbits, r.N, r.person_mode, r.digit_base, r.seg, r.status, \
+                      r.ctl, r.error, r.skip
         if (P == 1 && implicit)
             k_radix_pass<kRadixOnly><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
         else if (p == 0 && implicit)
@@ -1025,14 +1060,15 @@ __global__ void k_mark_buckets(const InstConst *ic, const InstState *is, const u
 // block per pair; weekend: 32 persons a round, one per lane), so key writes are
 // coalesced.  The kernel writes every person's keys, accumulates the radix digit
 // histograms of the entries of marked buckets in shared memory, and appends those
-// entries as (key, person) in ascending person order (warp scans + block scan +
-// decoupled look-back): the order the radix sort needs for stability.  Per-round
+// entries as (instance-local key, person) in ascending person order (warp scans +
+// block scan + decoupled look-back) to the instance's segment: the order the radix
+// sort needs for stability.  Per-round
 // marked counts of a lane are packed in one register between the two phases.  The
 // instance's constants are staged in shared memory.
 constexpr int kSchedThreads = 256, kSchedTile = kPersonTile, kSchedWarpPersons = 512;
 
 template <bool WEEKEND>
-__global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic, const InstState *is,
+__global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic, InstState *is,
                                                          const int32_t *tile_inst, int K, const uint8_t *age,
                                                          const uint32_t *mark, int32_t *keys, int *digit_hist,
                                                          int passes, uint32_t *ckeys, uint32_t *cvals, Scalars *sc,
@@ -1092,7 +1128,7 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
             }
             const int cnt = (int)mk[0] + (int)mk[1] + (int)mk[2];
 #pragma unroll
-            for (int k = 0; k < 3; k++) digit_count(s_dh, passes, mk[k], kb[k]);
+            for (int k = 0; k < 3; k++) digit_count(s_dh, passes, mk[k], kb[k] - (uint32_t)bb);
             cpack |= (uint32_t)cnt << (kBits * j);
             mine += cnt;
         }
@@ -1122,7 +1158,7 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
             }
             const int cnt = (int)mk[0] + (int)mk[1] + (int)mk[2] + (int)mk[3];
 #pragma unroll
-            for (int k = 0; k < 4; k++) digit_count(s_dh, passes, mk[k], kb[k]);
+            for (int k = 0; k < 4; k++) digit_count(s_dh, passes, mk[k], kb[k] - (uint32_t)bb);
             cpack |= (uint32_t)cnt << (kBits * j);
             mine += cnt;
         }
@@ -1136,29 +1172,29 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
     if (lane == 0) s_wtot[warp] = wt;
     __syncthreads();
     if (warp == 0) {
+        // the instance's entries form their own segment: its first tile starts the scan
         int tot = 0;
         for (int w = 0; w < kSchedThreads / 32; w++) tot += s_wtot[w];
-        const unsigned prefix = lookback_publish_warp(lb, epoch, tile, (unsigned)tot);
+        const unsigned prefix = lookback_publish_warp(lb, epoch, tile, (unsigned)tot, tbase == 0);
         if (lane == 0) {
             int run = (int)prefix;
             for (int w = 0; w < kSchedThreads / 32; w++) {
                 s_wbase[w] = run;
                 run += s_wtot[w];
             }
-            if (tile == (int)gridDim.x - 1) {
-                sc->marked_entries = run;
-                sc->materialised_sum += (unsigned long long)run;
-            }
+            if (pbase + tbase + kSchedTile == ti.pend) is[inst].marked = run;
         }
     }
     __syncthreads();
     {
-        int *h = digit_hist + (size_t)(blockIdx.x % kDigitStripes) * kMaxRadixPasses * 256;
+        int *h = digit_hist + ((size_t)inst * kDigitStripes + blockIdx.x % kDigitStripes) * kMaxRadixPasses * 256;
         for (int p = 0; p < passes; p++) {
             const int v = s_dh[p][threadIdx.x];
             if (v) red_add(&h[p * 256 + threadIdx.x], v);
         }
     }
+    ckeys += ic[inst].kbase;   // the instance's segment of the entry arrays
+    cvals += ic[inst].kbase;
     // append the marked entries, rounds in order, lanes in order within a round
     int run = s_wbase[warp];
     const uint32_t cmask = (1u << kBits) - 1u;
@@ -1176,7 +1212,7 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
                 for (int k = 0; k < 3; k++) {
                     const uint32_t b = (uint32_t)kk[3 * (size_t)(tbase + i) + k];
                     if (is_marked(mark, (int)b)) {
-                        ckeys[pos] = b;
+                        ckeys[pos] = b - (uint32_t)bb;
                         cvals[pos] = (uint32_t)(gbase + i);
                         pos++;
                     }
@@ -1190,7 +1226,7 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
                         for (int h = 0; h < 2; h++) {
                             const uint32_t b = (uint32_t)kk[(size_t)h * NK + tbase + i + k];
                             if (is_marked(mark, (int)b)) {
-                                ckeys[pos] = b;
+                                ckeys[pos] = b - (uint32_t)bb;
                                 cvals[pos] = (uint32_t)(gbase + i + k);
                                 pos++;
                             }
@@ -1224,7 +1260,7 @@ cudaError_t launch_schedule(const DevArrays &d, bool weekend, int day, bool full
     }
     const int blocks = d.P / kSchedTile;
     const LookBack lb = make_lb(d);
-    const int passes = radix_passes(B);
+    const int passes = radix_passes(d.bucket_max[weekend ? 1 : 0]);
     if (weekend)
         k_sched<true><<<blocks, kSchedThreads, 0, s>>>(
             d.ic, d.is, d.tile_inst, d.K, d.age, d.mark, d.keys, d.digit_hist, passes, d.rk1, d.rv1, d.sc, lb, day);
@@ -1235,21 +1271,26 @@ cudaError_t launch_schedule(const DevArrays &d, bool weekend, int day, bool full
     return cudaGetLastError();
 }
 
-// The day's radix sort starts from the marked entries the schedule appended to
-// (rk1, rv1), in person order; their count is on the device.
+// The day's radix sort starts from the marked entries the schedule appended to each
+// instance's segment of (rk1, rv1), in person order: one sorted segment per instance,
+// keys local to the instance, so the passes cover the largest instance's buckets
+// only.
 static RadixArgs day_radix_args(const DevArrays &d, bool weekend)
 {
     RadixArgs r;
     r.keys = d.rk1;
     r.vals = d.rv1;
-    r.E = (weekend ? 3 : 2) * d.P;
-    r.buckets = d.buckets[weekend ? 1 : 0];
+    r.E = 3 * d.P;   // at most (sizes the persistent grid)
+    r.buckets = d.bucket_max[weekend ? 1 : 0];
     r.N = d.P;
     r.person_mode = weekend ? 2 : 1;
-    r.count_dev = &d.sc->marked_entries;
     r.k0 = d.rk0; r.v0 = d.rv0; r.k1 = d.rk1; r.v1 = d.rv1;
     r.out = (uint32_t *)d.bkt_people;
     r.digit_base = d.digit_base;
+    r.seg.tile_prefix = d.tile_prefix;
+    r.seg.ic = d.ic;
+    r.seg.is = d.is;
+    r.seg.segments = d.K;
     r.status = d.radix_status;
     r.ctl = d.radix_ctl;
     r.error = &d.sc->error;
@@ -1258,36 +1299,90 @@ static RadixArgs day_radix_args(const DevArrays &d, bool weekend)
     return r;
 }
 
-// The schedule kernel accumulated the digit histograms of the marked entries; their
-// exclusive scans are the radix passes' digit bases.
+// One block per instance: the digit bases of its segment from the digit histograms
+// the schedule kernel accumulated (summing the stripes, clearing them).  Block 0
+// also numbers the segments' radix tiles (tile_prefix) and adds the day's
+// materialised entries to the running total.
+__global__ void k_day_digit_bases(int *digit_hist, int *digit_base, int passes, const InstState *is, int K,
+                                  int32_t *tile_prefix, Scalars *sc)
+{
+    if (*(volatile const int *)&sc->done) return;
+    const int k = blockIdx.x;
+    for (int p = 0; p < passes; p++) {
+        int v = 0;
+        for (int st = 0; st < kDigitStripes; st++) {
+            int *h = &digit_hist[(((size_t)k * kDigitStripes + st) * kMaxRadixPasses + p) * 256 + threadIdx.x];
+            v += *h;
+            *h = 0;
+        }
+        int total;
+        const int excl = block_exclusive_scan<256, int>(v, total);
+        digit_base[((size_t)k * passes + p) * 256 + threadIdx.x] = excl;
+    }
+    if (k != 0) return;
+    int carry = 0;
+    unsigned long long entries = 0;
+    for (int b = 0; b < K; b += 256) {
+        const int i = b + (int)threadIdx.x;
+        const int m = i < K ? is[i].marked : 0;
+        int total;
+        const int excl = block_exclusive_scan<256, int>((m + kRadixTile - 1) / kRadixTile, total);
+        if (i < K) tile_prefix[i] = carry + excl;
+        carry += total;
+        int msum;
+        block_exclusive_scan<256, int>(m, msum);
+        entries += (unsigned long long)msum;
+    }
+    if (threadIdx.x == 0) {
+        tile_prefix[K] = carry;
+        sc->materialised_sum += entries;
+    }
+}
+
 cudaError_t launch_bucket_scan(const DevArrays &d, bool weekend, cudaStream_t s)
 {
-    const int P = radix_passes(d.buckets[weekend ? 1 : 0]);
-    k_digit_bases<<<1, 256, 0, s>>>(d.digit_hist, d.digit_base, P, kDigitStripes, &d.sc->done);
+    const int P = radix_passes(d.bucket_max[weekend ? 1 : 0]);
+    k_day_digit_bases<<<d.K, 256, 0, s>>>(d.digit_hist, d.digit_base, P, d.is, d.K, d.tile_prefix, d.sc);
     count_launch();
     return cudaGetLastError();
 }
 
-// Bucket offsets from the sorted keys of the day's materialised entries: entry i
-// starts bucket keys[i] when that differs from keys[i-1] (thrust::lower_bound in
-// the reference, PandemicSim.cu:1240-1248).  Lazy tables write only the offsets the
+// Bucket offsets from the sorted keys of each instance's segment: entry i starts
+// bucket keys[i] when that differs from keys[i-1] (thrust::lower_bound in the
+// reference, PandemicSim.cu:1240-1248).  Lazy tables write only the offsets the
 // infection kernels read: the start of each bucket with entries and the end of the
 // bucket before it.  Every bucket an infected person reads holds that person, so it
-// has entries.  Complete tables write every offset, empty buckets included.
-__global__ void k_bucket_offsets(const uint32_t *keys, const int *count_dev, int B, int full, int32_t *offset,
+// has entries.  Complete tables write every offset, empty buckets included.  Offsets
+// are positions in the batch's bucketed person array; each instance's last offset
+// goes to its own end slot.
+__global__ void k_bucket_offsets(const uint32_t *keys, RadixSegments sg, int weekend, int full, int32_t *offset,
                                  const int *skip)
 {
     if (*(volatile const int *)skip) return;
-    const int E = *count_dev;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= E; i += gridDim.x * blockDim.x) {
-        const int prev = i == 0 ? -1 : (int)keys[i - 1];
-        const int cur = i == E ? B : (int)keys[i];
-        if (prev == cur) continue;
-        if (full) {
-            for (int b = prev + 1; b <= cur; b++) offset[b] = i;
-        } else {
-            offset[prev + 1] = i;
-            offset[cur] = i;
+    const int tiles = sg.tile_prefix[sg.segments];
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+        int lo = 0, hi = sg.segments - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (sg.tile_prefix[mid] <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        const InstConst &c = sg.ic[lo];
+        const int m = sg.is[lo].marked;
+        const int sbase = (int)c.kbase, bb = c.bbase[weekend], B = c.bcount[weekend];
+        const int first = (t - sg.tile_prefix[lo]) * kRadixTile;
+        int last = first + kRadixTile < m ? first + kRadixTile : m;
+        if (last == m) last = m + 1;  // the segment's last tile also writes the end offset
+        for (int i = first + (int)threadIdx.x; i < last; i += blockDim.x) {
+            const int prev = i == 0 ? -1 : (int)keys[sbase + i - 1];
+            const int cur = i == m ? B : (int)keys[sbase + i];
+            if (prev == cur) continue;
+            if (full) {
+                for (int b = prev + 1; b <= cur; b++) offset[bb + b] = sbase + i;
+            } else {
+                offset[bb + prev + 1] = sbase + i;
+                offset[bb + cur] = sbase + i;
+            }
         }
     }
 }
@@ -1299,7 +1394,7 @@ cudaError_t launch_bucket_sort(const DevArrays &d, bool weekend, bool full_table
     if (e != cudaSuccess) return e;
     const int P = radix_passes(r.buckets);
     const uint32_t *sorted = ((P - 1) & 1) ? r.k1 : r.k0;  // where the last pass wrote the keys
-    k_bucket_offsets<<<sm_count() * 8, 256, 0, s>>>(sorted, r.count_dev, r.buckets, full_tables ? 1 : 0,
+    k_bucket_offsets<<<sm_count() * 8, 256, 0, s>>>(sorted, r.seg, weekend ? 1 : 0, full_tables ? 1 : 0,
                                                     d.bkt_offset, r.skip);
     count_launch();
     return cudaGetLastError();

@@ -38,6 +38,8 @@ struct InstConst {
                            // holds the padding persons
     int lbase;             // first global location
     int bbase[2];          // first global bucket of the weekday / weekend errand tables
+    int bcount[2];         // the instance's weekday / weekend buckets; one more global
+                           // slot follows them (the end offset of its last bucket)
     int max_days;
     long long kbase;       // first schedule-key slot (3 * pbase)
 };
@@ -51,6 +53,7 @@ struct InstState {
     int infected;                       // infected count of the current day
     int start;                          // their first position in the batch's infected list
     int list_end;                       // one past their last position
+    int marked;                         // today's schedule entries in materialised buckets
     int done;                           // set once a day counts zero infected
     int days_run;                       // statistics rows written
     int day;                            // last day run
@@ -67,7 +70,6 @@ struct Scalars {
     int new_count;                        // entries in the new-infection list
     int error;                            // nonzero: a bounded device wait gave up
     int error_site;
-    int marked_entries;                   // schedule entries in today's materialised buckets
     int pad;
 };
 
@@ -84,14 +86,15 @@ struct DevArrays {
     int32_t *wp_people;       // P (padding persons last, in the spare bucket)
     int32_t *wp_offset;       // locations + 2
     int32_t *keys;            // 3P schedule keys (global bucket indices)
-    int32_t *bkt_offset;      // buckets+1
+    int32_t *bkt_offset;      // buckets (each instance's buckets and its end slot)
     int32_t *bkt_count;       // buckets histogram, zero between uses
     int32_t *bkt_people;      // 3P person ids bucket by bucket, ascending in each
     uint32_t *rk0, *rv0, *rk1, *rv1;  // 3P each: radix ping-pong keys/values
     unsigned long long *radix_status;  // ceil(3P/4096) x 256 epoch-tagged look-back words
     int *radix_ctl;           // ticket, finished
-    int *digit_hist;          // kDigitStripes x 4 x 256
-    int *digit_base;          // 4 x 256
+    int *digit_hist;          // K x kDigitStripes x 4 x 256 (the first 4 x 256 also serve the setup sorts)
+    int *digit_base;          // K x 4 x 256
+    int32_t *tile_prefix;     // K + 1: radix tiles of the instances' segments
     uint32_t *mark;           // bitmap over today's buckets: 1 = materialise
     int32_t *infected;        // P ascending infected ids
     int32_t *infected_inst;   // P: instance of each infected list position
@@ -104,7 +107,8 @@ struct DevArrays {
     const int32_t *tile_inst; // P / kPersonTile: instance of each person tile
     int K;
     int P;                    // persons including padding, a multiple of kPersonTile
-    int buckets[2];           // weekday / weekend buckets over all instances
+    int buckets[2];           // weekday / weekend bucket slots over all instances
+    int bucket_max[2];        // largest weekday / weekend bucket count of one instance
     int locations;            // locations over all instances
     Scalars *sc;
 };
@@ -129,6 +133,17 @@ cudaError_t launch_batch_padding(const DevArrays &d, uint8_t *types, int32_t *si
                                  bool persons, cudaStream_t s);
 cudaError_t launch_count_keys(const int32_t *keys, int n, int32_t *count, cudaStream_t s);
 
+// Segments of a day's sort: segment k (instance k) holds its entries at
+// [ic[k].kbase, ic[k].kbase + is[k].marked), keys local to the instance, sorted within
+// the segment; its tiles are [tile_prefix[k], tile_prefix[k + 1]).  tile_prefix ==
+// nullptr: one segment [0, E).
+struct RadixSegments {
+    const int *tile_prefix = nullptr;   // segments + 1, on the device
+    const InstConst *ic = nullptr;
+    const InstState *is = nullptr;
+    int segments = 0;
+};
+
 // Stable LSD radix sort of E keys in [0, buckets) with implicit person values
 // (person_mode 0: entry i is person i; 1: weekday hour-major; 2: weekend 3 per person).
 struct RadixArgs {
@@ -139,7 +154,8 @@ struct RadixArgs {
     const int *count_dev = nullptr;   // entry count after the filter (device)
     uint32_t *k0, *v0, *k1, *v1, *out;
     bool keep_keys = false;       // the last pass also writes the sorted keys (to k0 / k1 by pass parity)
-    const int *digit_base;
+    const int *digit_base;        // [segment][pass][256]
+    RadixSegments seg;
     unsigned long long *status;   // look-back words, ceil(E/4096) x 256, epoch-tagged
     int *ctl;                     // ticket, finished, epoch
     int *error;

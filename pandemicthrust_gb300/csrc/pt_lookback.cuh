@@ -29,12 +29,15 @@ __device__ __forceinline__ unsigned long long lb_word(unsigned epoch, unsigned f
 // Called by all 32 lanes of one warp.  Publishes the tile aggregate, then walks back
 // 32 predecessors per step (one word per lane) to the nearest inclusive prefix,
 // publishes the tile's inclusive prefix and returns the exclusive one on every lane.
-static __device__ unsigned lookback_publish_warp(const LookBack &lb, unsigned epoch, int tile, unsigned aggregate)
+// A tile that starts a segment (segment_start) publishes its aggregate as its
+// inclusive prefix: the scans of consecutive segments are independent.
+static __device__ unsigned lookback_publish_warp(const LookBack &lb, unsigned epoch, int tile, unsigned aggregate,
+                                                 bool segment_start = false)
 {
     volatile unsigned long long *t = lb.tiles;
     const int lane = threadIdx.x & 31;
-    if (tile == 0) {
-        if (lane == 0) t[0] = lb_word(epoch, 2, aggregate);
+    if (tile == 0 || segment_start) {
+        if (lane == 0) t[tile] = lb_word(epoch, 2, aggregate);
         return 0;
     }
     if (lane == 0) t[tile] = lb_word(epoch, 1, aggregate);

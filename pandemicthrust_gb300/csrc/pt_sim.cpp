@@ -217,8 +217,8 @@ static pt_status engine_setup(Engine *s)
         bbase1[k] = (int)B1;
         HS += (long long)c.H + 1;
         LT += c.L;
-        B0 += ptk::day_buckets(c, false);
-        B1 += ptk::day_buckets(c, true);
+        B0 += ptk::day_buckets(c, false) + 1;  // each instance's buckets and its end slot
+        B1 += ptk::day_buckets(c, true) + 1;
         maxP += 5ll * c.H + ptk::kPersonTile;  // the largest household type holds 5 persons
         if (HS + 1 > INT_MAX / 2 || LT + 2 > INT_MAX / 2 || B1 + 1 > INT_MAX / 2 || maxP > INT_MAX)
             return fail(s, PT_ERR_ARG, "batch too large for 32-bit ids");
@@ -282,6 +282,7 @@ static pt_status engine_setup(Engine *s)
     }
     if (3 * P >= (long long)INT_MAX) return fail(s, PT_ERR_ARG, "batch too large (3 x persons must stay below 2^31)");
     s->ic.resize(K);
+    d.bucket_max[0] = d.bucket_max[1] = 1;
     for (int k = 0; k < K; k++) {
         ptk::InstConst &r = s->ic[k];
         std::memset(&r, 0, sizeof(r));
@@ -292,6 +293,10 @@ static pt_status engine_setup(Engine *s)
         r.lbase = lbase[k];
         r.bbase[0] = bbase0[k];
         r.bbase[1] = bbase1[k];
+        r.bcount[0] = ptk::day_buckets(r.c, false);
+        r.bcount[1] = ptk::day_buckets(r.c, true);
+        d.bucket_max[0] = std::max(d.bucket_max[0], r.bcount[0]);
+        d.bucket_max[1] = std::max(d.bucket_max[1], r.bcount[1]);
         r.max_days = s->inst[k].params.max_days;
         r.kbase = 3ll * pbase[k];
     }
@@ -309,7 +314,7 @@ static pt_status engine_setup(Engine *s)
 
     // arena of per-person and per-location arrays
     const size_t n = (size_t)P, ntiles = n / ptk::kPersonTile;
-    const size_t radix_tiles = (3 * n + 4095) / 4096 + 1;
+    const size_t radix_tiles = (3 * n + 4095) / 4096 + 1 + (size_t)K;  // segments round up to whole tiles
     int nseeds = 0;
     for (const Instance &in : s->inst) nseeds += in.params.initial_pandemic + in.params.initial_seasonal;
     size_t bytes = 0;
@@ -321,7 +326,9 @@ static pt_status engine_setup(Engine *s)
     bytes += round256(((size_t)Bday + 1) * 4);  // bkt_offset
     bytes += round256((size_t)Bmax * 4);        // bkt_count (also the workplace histogram)
     bytes += round256(radix_tiles * 256 * 8);   // radix look-back words
-    bytes += round256(8 * 4) + round256((size_t)ptk::kDigitStripes * 4 * 256 * 4) + round256(4 * 256 * 4);  // radix ctl, digit hist/base
+    bytes += round256(8 * 4);                                                      // radix ctl
+    bytes += round256((size_t)K * ptk::kDigitStripes * 4 * 256 * 4);               // digit histograms
+    bytes += round256((size_t)K * 4 * 256 * 4) + round256(((size_t)K + 1) * 4);  // digit bases, tile prefix
     bytes += round256(((size_t)Bday / 32 + 1) * 4);        // bucket mark bitmap
     bytes += round256(n * 4) * 2;               // infected, infected_inst
     bytes += round256(2 * n * 8);               // claim
@@ -349,8 +356,9 @@ static pt_status engine_setup(Engine *s)
     d.bkt_count = a.take<int32_t>((size_t)Bmax);
     d.radix_status = a.take<unsigned long long>(radix_tiles * 256);
     d.radix_ctl = a.take<int>(8);
-    d.digit_hist = a.take<int>((size_t)ptk::kDigitStripes * 4 * 256);
-    d.digit_base = a.take<int>(4 * 256);
+    d.digit_hist = a.take<int>((size_t)K * ptk::kDigitStripes * 4 * 256);
+    d.digit_base = a.take<int>((size_t)K * 4 * 256);
+    d.tile_prefix = a.take<int32_t>((size_t)K + 1);
     d.mark = a.take<uint32_t>((size_t)Bday / 32 + 1);
     d.infected = a.take<int32_t>(n);
     d.infected_inst = a.take<int32_t>(n);
@@ -372,7 +380,7 @@ static pt_status engine_setup(Engine *s)
     CK(cudaMemsetAsync(d.bkt_count, 0, (size_t)Bmax * 4, s->stream), "memset counts");
     CK(cudaMemsetAsync(d.radix_ctl, 0, 8 * 4, s->stream), "memset radix ctl");
     CK(cudaMemsetAsync(d.radix_status, 0, radix_tiles * 256 * 8, s->stream), "memset radix words");
-    CK(cudaMemsetAsync(d.digit_hist, 0, (size_t)ptk::kDigitStripes * 4 * 256 * 4, s->stream), "memset digit hist");
+    CK(cudaMemsetAsync(d.digit_hist, 0, (size_t)K * ptk::kDigitStripes * 4 * 256 * 4, s->stream), "memset digit hist");
 
     // households -> persons, padding persons, then workplaces and schools (setup_assignWorkplaces)
     CK(ptk::launch_generate_households(types, d.hh_offset, (int)HS, d.household, d.age, s->stream), "households");
