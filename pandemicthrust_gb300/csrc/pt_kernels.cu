@@ -709,43 +709,6 @@ __device__ __forceinline__ uint32_t recover_word(uint32_t st, int d2r, bool &cha
     return out;
 }
 
-// End of the sweep, run by the last block to finish: each running instance's day
-// bookkeeping (runToCompletion, PandemicSim.cu:891-937: the statistics row, the stop
-// on zero infected, the counter offsets E0 / R0 of the schedule and the contacts).
-// An instance's infected are the positions [start, list_end) of today's list,
-// recorded by its first and last tiles.
-__device__ void sweep_day_end(const InstConst *ic, InstState *is, int K, Scalars *sc, int day)
-{
-    const bool weekend = (day % 7) >= 5;  // PandemicSim.h:283-284
-    for (int k = threadIdx.x; k < K; k += kSweepThreads) {
-        InstState &s = is[k];
-        if (!instance_running(ic[k], s, day)) {
-            s.infected = 0;
-            continue;
-        }
-        const int I = *(volatile int *)&s.list_end - *(volatile int *)&s.start;
-        s.infected = I;
-        s.infected_per_day[day] = I;
-        s.day = day;
-        s.days_run = day + 1;
-        if (I == 0) {
-            s.done = 1;
-        } else {
-            const unsigned long long N = (unsigned long long)ic[k].c.N;
-            const unsigned long long E0 = s.rand_offset;
-            const unsigned long long R0 = E0 + (weekend ? 2ull * N : N / 2ull);
-            s.errand_offset = E0;
-            s.infect_offset = R0;
-            s.rand_offset = R0 + 6ull * (unsigned long long)I;
-        }
-    }
-    if (threadIdx.x == 0) {
-        sc->day = day;
-        sc->new_count = 0;
-        if (*(volatile int *)&sc->infected == 0) sc->done = 1;
-    }
-}
-
 // A day kernel's person tile: its look-back ticket and the instance it belongs to.
 // Thread 0 takes the ticket; with a single instance the instance record is read in
 // parallel with the ticket's round trip instead of after it.
@@ -786,28 +749,34 @@ __device__ __forceinline__ void tile_begin(const LookBack &lb, const InstConst *
     out = s_t;
 }
 
-// kernel_countInfectedStatusAndRecover (PandemicSim.cu:2097-2192) and the copy_if
-// of the infected (:2207-2224) in one pass: recover, count the 16 status bins of the
-// instance, and write the ascending infected list by a decoupled look-back.
-__global__ void __launch_bounds__(kSweepThreads, 8) k_sweep(const InstConst *ic, InstState *is, const int32_t *tile_inst,
-                                                         int K, uint32_t *state, int32_t *infected,
-                                                         int32_t *infected_inst, Scalars *sc, LookBack lb, int day)
+// The sweep: kernel_countInfectedStatusAndRecover (PandemicSim.cu:2097-2192), the
+// copy_if of the infected (:2207-2224) and runToCompletion's day bookkeeping
+// (:891-937) in three launches over every instance:
+//   count  one person tile per block: recover, count the instance's 16 status bins,
+//          and record each thread's infected persons as a 16-bit mask and the
+//          tile's infected count.  Thread t of a tile holds persons
+//          (r * 256 + t) * 4 + j, rounds r = 0..3, items j = 0..3; mask bit 4r + j.
+//   scan   one block: exclusive scan of the tile counts, each instance's run
+//          [start, list_end) of the infected list and its day bookkeeping.
+//   emit   one person tile per block: the infected ids, in ascending order, at
+//          their list positions.
+// Each launch depends only on the one before, so no block waits for another.
+__global__ void __launch_bounds__(kSweepThreads, 8) k_sweep_count(const InstConst *ic, InstState *is,
+                                                                  const int32_t *tile_inst, uint32_t *state,
+                                                                  uint16_t *flags_out, int32_t *tile_count,
+                                                                  const Scalars *sc, int day)
 {
-    if (*(volatile int *)&sc->done) return;
-    TileInfo ti;
-    tile_begin(lb, ic, is, tile_inst, K, day, ti);
-    const int tile = ti.tile;
-    const unsigned epoch = ti.epoch;
-    const int k = ti.inst;
+    if (*(volatile const int *)&sc->done) return;
+    const int tile = blockIdx.x;
+    const int k = tile_inst[tile];
     const long long tile_base = (long long)tile * kSweepTile;
     // end of the tile's persons: none when the instance no longer runs
-    const long long N = ti.first_person_after;
+    const long long N = instance_running(ic[k], is[k], day) ? (long long)ic[k].pbase + ic[k].c.N : tile_base;
     const int d2r = day - 10;
     // packed per-thread status bins: 16-bit fields, bins 0-3 / 4-7 per strain
     unsigned long long bp_lo = 0, bp_hi = 0, bs_lo = 0, bs_hi = 0;
     int nss = 0;         // persons in the never-infected state (S, S, day 255, day 255)
     uint32_t flags = 0;  // bit (4*round + item)
-    unsigned long long packed_counts = 0;
 #pragma unroll
     for (int r = 0; r < kSweepRounds; r++) {
         long long p0 = tile_base + ((long long)r * kSweepThreads + threadIdx.x) * 4;
@@ -821,7 +790,6 @@ __global__ void __launch_bounds__(kSweepThreads, 8) k_sweep(const InstConst *ic,
         }
         bool any_changed = false;
         uint32_t out[4];
-        int cnt = 0;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             // never infected by either strain: nothing to recover, bin S twice
@@ -837,10 +805,7 @@ __global__ void __launch_bounds__(kSweepThreads, 8) k_sweep(const InstConst *ic,
                 uint32_t sp = out[j] & 0xFFu, ss = (out[j] >> 8) & 0xFFu;
                 if (sp < 4) bp_lo += 1ull << (16 * sp); else bp_hi += 1ull << (16 * (sp - 4));
                 if (ss < 4) bs_lo += 1ull << (16 * ss); else bs_hi += 1ull << (16 * (ss - 4));
-                if (sp >= 2u || ss >= 2u) {
-                    flags |= 1u << (4 * r + j);
-                    cnt++;
-                }
+                if (sp >= 2u || ss >= 2u) flags |= 1u << (4 * r + j);
             }
         }
         if (any_changed) {
@@ -852,13 +817,15 @@ __global__ void __launch_bounds__(kSweepThreads, 8) k_sweep(const InstConst *ic,
                     if (p0 + j < N) state[p0 + j] = out[j];
             }
         }
-        packed_counts |= (unsigned long long)cnt << (16 * r);
     }
-    // status bins: warp reduction then one atomic per bin per warp
+    flags_out[(size_t)tile * kSweepThreads + threadIdx.x] = (uint16_t)flags;
+    // status bins and the tile's infected count: warp reductions, then one atomic
+    // per bin per warp
     bp_lo += (unsigned long long)nss << 16;  // bin 1 (S) of each strain
     bs_lo += (unsigned long long)nss << 16;
-    __shared__ int s_bins[16];
-    if (threadIdx.x < 16) s_bins[threadIdx.x] = 0;
+    int cnt = __popc(flags);
+    __shared__ int s_bins[17];
+    if (threadIdx.x < 17) s_bins[threadIdx.x] = 0;
     __syncthreads();
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -866,6 +833,7 @@ __global__ void __launch_bounds__(kSweepThreads, 8) k_sweep(const InstConst *ic,
         bp_hi += __shfl_xor_sync(0xffffffffu, bp_hi, o);
         bs_lo += __shfl_xor_sync(0xffffffffu, bs_lo, o);
         bs_hi += __shfl_xor_sync(0xffffffffu, bs_hi, o);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
     }
     if ((threadIdx.x & 31) == 0) {
 #pragma unroll
@@ -877,61 +845,102 @@ __global__ void __launch_bounds__(kSweepThreads, 8) k_sweep(const InstConst *ic,
             if (a2) atomicAdd(&s_bins[8 + b], a2);
             if (a3) atomicAdd(&s_bins[12 + b], a3);
         }
-    }
-    // ordered compaction: scan the four per-round counts at once (16-bit fields)
-    unsigned long long round_tot;
-    unsigned long long excl = block_exclusive_scan<kSweepThreads, unsigned long long>(packed_counts, round_tot);
-    unsigned tile_total = 0;
-    unsigned round_base[kSweepRounds];
-#pragma unroll
-    for (int r = 0; r < kSweepRounds; r++) {
-        round_base[r] = tile_total;
-        tile_total += (unsigned)((round_tot >> (16 * r)) & 0xFFFF);
-    }
-    __shared__ unsigned s_prefix;
-    if (threadIdx.x < 32) {
-        const unsigned e = lookback_publish_warp(lb, epoch, tile, tile_total);
-        if (threadIdx.x == 0) s_prefix = e;
+        if (cnt) atomicAdd(&s_bins[16], cnt);
     }
     __syncthreads();
-    const unsigned prefix = s_prefix;
+    if (threadIdx.x < 16 && s_bins[threadIdx.x]) atomicAdd(&is[k].counts[day][threadIdx.x], s_bins[threadIdx.x]);
+    if (threadIdx.x == 16) tile_count[tile] = s_bins[16];
+}
+
+constexpr int kSweepScanThreads = 1024;
+
+__global__ void __launch_bounds__(kSweepScanThreads) k_sweep_scan(const InstConst *ic, InstState *is, int K,
+                                                                  int32_t *tile_count, int tiles, Scalars *sc,
+                                                                  int day)
+{
+    if (*(volatile const int *)&sc->done) return;
+    // exclusive scan in place, a contiguous chunk per thread; entry `tiles` = total
+    const int per = (tiles + kSweepScanThreads - 1) / kSweepScanThreads;
+    const int lo = (int)threadIdx.x * per, hi = lo + per < tiles ? lo + per : tiles;
+    int sum = 0;
+    for (int i = lo; i < hi; i++) sum += tile_count[i];
+    int total;
+    int run = block_exclusive_scan<kSweepScanThreads, int>(sum, total);
+    for (int i = lo; i < hi; i++) {
+        const int v = tile_count[i];
+        tile_count[i] = run;
+        run += v;
+    }
+    if (threadIdx.x == 0) tile_count[tiles] = total;
+    __syncthreads();
+    // each running instance's day (runToCompletion, PandemicSim.cu:891-937: the
+    // statistics row, the stop on zero infected, the counter offsets E0 / R0 of the
+    // schedule and the contacts)
+    const bool weekend = (day % 7) >= 5;  // PandemicSim.h:283-284
+    for (int k = threadIdx.x; k < K; k += kSweepScanThreads) {
+        InstState &s = is[k];
+        const int start = tile_count[ic[k].pbase / kSweepTile], end = tile_count[ic[k].pend / kSweepTile];
+        s.start = start;
+        s.list_end = end;
+        if (!instance_running(ic[k], s, day)) {
+            s.infected = 0;
+            continue;
+        }
+        const int I = end - start;
+        s.infected = I;
+        s.infected_per_day[day] = I;
+        s.day = day;
+        s.days_run = day + 1;
+        if (I == 0) {
+            s.done = 1;
+        } else {
+            const unsigned long long N = (unsigned long long)ic[k].c.N;
+            const unsigned long long E0 = s.rand_offset;
+            const unsigned long long R0 = E0 + (weekend ? 2ull * N : N / 2ull);
+            s.errand_offset = E0;
+            s.infect_offset = R0;
+            s.rand_offset = R0 + 6ull * (unsigned long long)I;
+        }
+    }
+    if (threadIdx.x == 0) {
+        sc->infected = total;
+        sc->day = day;
+        sc->new_count = 0;
+        if (total == 0) sc->done = 1;
+    }
+}
+
+__global__ void __launch_bounds__(kSweepThreads) k_sweep_emit(const int32_t *tile_inst, const uint16_t *flags_in,
+                                                              const int32_t *tile_prefix, int32_t *infected,
+                                                              int32_t *infected_inst, const Scalars *sc)
+{
+    if (*(volatile const int *)&sc->done) return;
+    const int tile = blockIdx.x;
+    const int prefix = tile_prefix[tile];
+    if (tile_prefix[tile + 1] == prefix) return;  // no infected in this tile
+    const uint32_t f = flags_in[(size_t)tile * kSweepThreads + threadIdx.x];
+    unsigned long long packed = 0;
+#pragma unroll
+    for (int r = 0; r < kSweepRounds; r++) packed |= (unsigned long long)__popc((f >> (4 * r)) & 0xFu) << (16 * r);
+    // positions in person order: scan the four per-round counts at once (16-bit fields)
+    unsigned long long round_tot;
+    const unsigned long long excl = block_exclusive_scan<kSweepThreads, unsigned long long>(packed, round_tot);
+    const int k = tile_inst[tile];
+    const long long tile_base = (long long)tile * kSweepTile;
+    int round_base = prefix;
 #pragma unroll
     for (int r = 0; r < kSweepRounds; r++) {
-        unsigned pos = prefix + round_base[r] + (unsigned)((excl >> (16 * r)) & 0xFFFF);
-        long long p0 = tile_base + ((long long)r * kSweepThreads + threadIdx.x) * 4;
+        int pos = round_base + (int)((excl >> (16 * r)) & 0xFFFF);
+        const long long p0 = tile_base + ((long long)r * kSweepThreads + threadIdx.x) * 4;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            if (flags & (1u << (4 * r + j))) {
+            if (f & (1u << (4 * r + j))) {
                 infected[pos] = (int32_t)(p0 + j);
                 infected_inst[pos] = k;
                 pos++;
             }
         }
-    }
-    if (threadIdx.x < 16 && s_bins[threadIdx.x]) atomicAdd(&is[k].counts[day][threadIdx.x], s_bins[threadIdx.x]);
-    if (threadIdx.x == 0) {
-        // the instance's run of the infected list, and the list's length
-        if (tile_base == ti.pbase) is[k].start = (int)prefix;
-        if (tile_base + kSweepTile == ti.pend) is[k].list_end = (int)(prefix + tile_total);
-        if (tile == (int)gridDim.x - 1) sc->infected = (int)(prefix + tile_total);
-    }
-    // the last block to finish closes the day of every instance (the barrier, then
-    // one release fence, orders the block's updates before its finish count)
-    __syncthreads();
-    __shared__ int s_last;
-    if (threadIdx.x == 0) {
-        __threadfence();
-        s_last = atomicAdd(&lb.ctl[1], 1) == (int)gridDim.x - 1;
-    }
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    sweep_day_end(ic, is, K, sc, day);
-    if (threadIdx.x == 0) {
-        lb.ctl[0] = 0;
-        lb.ctl[1] = 0;
-        atomicAdd(&lb.ctl[2], 1);
-        __threadfence();
+        round_base += (int)((round_tot >> (16 * r)) & 0xFFFF);
     }
 }
 
@@ -947,9 +956,14 @@ static LookBack make_lb(const DevArrays &d)
 
 cudaError_t launch_sweep(const DevArrays &d, int day, cudaStream_t s)
 {
-    const int blocks = d.P / kSweepTile;
-    k_sweep<<<blocks, kSweepThreads, 0, s>>>(d.ic, d.is, d.tile_inst, d.K, d.state, d.infected, d.infected_inst, d.sc,
-                                             make_lb(d), day);
+    const int tiles = d.P / kSweepTile;
+    k_sweep_count<<<tiles, kSweepThreads, 0, s>>>(d.ic, d.is, d.tile_inst, d.state, d.sweep_flags, d.sweep_tiles,
+                                                  d.sc, day);
+    count_launch();
+    k_sweep_scan<<<1, kSweepScanThreads, 0, s>>>(d.ic, d.is, d.K, d.sweep_tiles, tiles, d.sc, day);
+    count_launch();
+    k_sweep_emit<<<tiles, kSweepThreads, 0, s>>>(d.tile_inst, d.sweep_flags, d.sweep_tiles, d.infected,
+                                                 d.infected_inst, d.sc);
     count_launch();
     return cudaGetLastError();
 }

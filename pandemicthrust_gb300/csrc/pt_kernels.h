@@ -98,6 +98,8 @@ struct DevArrays {
     uint32_t *mark;           // bitmap over today's buckets: 1 = materialise
     int32_t *infected;        // P ascending infected ids
     int32_t *infected_inst;   // P: instance of each infected list position
+    uint16_t *sweep_flags;    // P / 16: the sweep's per-thread infected masks
+    int32_t *sweep_tiles;     // P / kPersonTile + 1: infected per person tile, then their prefix
     unsigned long long *claim;// 2P (victim, strain) -> min attempt key
     int32_t *new_list;        // 2P first claims of the day
     unsigned long long *tiles;// look-back tile status words

@@ -331,6 +331,7 @@ static pt_status engine_setup(Engine *s)
     bytes += round256((size_t)K * 4 * 256 * 4) + round256(((size_t)K + 1) * 4);  // digit bases, tile prefix
     bytes += round256(((size_t)Bday / 32 + 1) * 4);        // bucket mark bitmap
     bytes += round256(n * 4) * 2;               // infected, infected_inst
+    bytes += round256(n / 16 * 2) + round256((ntiles + 1) * 4);  // sweep masks, sweep tile counts
     bytes += round256(2 * n * 8);               // claim
     bytes += round256(2 * n * 4);               // new_list
     bytes += round256((size_t)(nseeds + 1) * 4);  // seeds
@@ -362,6 +363,8 @@ static pt_status engine_setup(Engine *s)
     d.mark = a.take<uint32_t>((size_t)Bday / 32 + 1);
     d.infected = a.take<int32_t>(n);
     d.infected_inst = a.take<int32_t>(n);
+    d.sweep_flags = a.take<uint16_t>(n / 16);
+    d.sweep_tiles = a.take<int32_t>(ntiles + 1);
     d.claim = a.take<unsigned long long>(2 * n);
     d.new_list = a.take<int32_t>(2 * n);
     s->d_seeds = a.take<int32_t>((size_t)(nseeds + 1));
