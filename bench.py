@@ -46,20 +46,24 @@ FALLBACK_HBM_GBS = 6800.0
 # fields at their information size: status/day/gen/age 1 B, ids and offsets 4 B).
 # E = entries of the day's schedule (2N weekday, 3N weekend); Bc = buckets a day can
 # use (2 hours x locations of types 8-13 weekday, 10 hours x types 9-13 weekend).
-#   sweep     4N read (status + day, both strains) + 4I written (infected list)
-#   schedule  weekday 1N age read + 4E keys written; weekend 4E keys written
-#   scan      4Bc counts read + 4(Bc+1) offsets written
-#   sort      4E schedule read + 4E' bucket entries written, E' = entries of the
-#             buckets that the day's infected visit (the only ones materialised)
-#   infect    79 B per infected weekday, 52 B weekend
-#   apply     claim 8 B read + 8 B reset + state 4 B + generation 1 B per new infection
+#   sweep          4N read (status + day, both strains)
+#   infected_list  4I written (the ascending infected ids)
+#   schedule       weekday 1N age read + 4E keys written; weekend 4E keys written
+#   digit_bases    (no compulsory traffic: the radix bookkeeping of the sort)
+#   bucket_sort    4E schedule read + 4E' bucket entries written, E' = entries of the
+#                  buckets that the day's infected visit (the only ones materialised)
+#   bucket_offsets 4(Bc+1) offsets written (the reference's lower_bound output)
+#   infect         79 B per infected weekday, 52 B weekend
+#   apply          claim 8 B read + 8 B reset + state 4 B + generation 1 B per new infection
 def stage_bytes(stage, weekend, N, Bc, I_mean, new_mean=0.0, mat_frac=1.0):
     E = (3 if weekend else 2) * N
     return {
-        "sweep": 4 * N + 4 * I_mean,
+        "sweep": 4 * N,
+        "infected_list": 4 * I_mean,
         "schedule": (4 * E) if weekend else (N + 4 * E),
-        "bucket_scan": 8 * Bc,
+        "digit_bases": 0,
         "bucket_sort": 4 * E + 4 * E * mat_frac,
+        "bucket_offsets": 4 * (Bc + 1),
         "infect": (52 if weekend else 79) * I_mean,
         "apply": 21 * new_mean,
     }[stage]
@@ -418,7 +422,7 @@ def main():
         byt = (stage_bytes(name, False, N, Bc_wd, Imean_wd, new_wd, mat_frac) * nwd +
                stage_bytes(name, True, N, Bc_we, Imean_we, new_we, mat_frac) * nwe)
         breakdown[name] = {"ms": round(tot, 3), "share": round(tot / run_ms, 4) if run_ms else None,
-                           "GBps": round(byt / (tot / 1000.0) / 1e9, 1) if tot > 0 else None}
+                           "GBps": round(byt / (tot / 1000.0) / 1e9, 1) if tot > 0 and byt > 0 else None}
     dominant = max(pt.PandemicSim.STAGES, key=lambda n: stages["weekday"][n] + stages["weekend"][n])
     dom_ms = stages["weekday"][dominant] + stages["weekend"][dominant]
     dom_launches = nwd + nwe

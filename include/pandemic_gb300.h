@@ -143,13 +143,18 @@ pt_status pt_set_full_tables(pt_sim *sim, int enabled);
 
 /* Device time per stage, from CUDA events recorded on the simulation's stream
  * around each stage of every day run while timing is enabled (pt_set_timing).
- * ms[0..5] sum the weekday stages, ms[8..13] the weekend stages, in the order:
- * sweep, schedule, bucket scan, bucket radix sort, infection, apply.
+ * ms[0..7] sum the weekday stages, ms[8..15] the weekend stages, in the order:
+ * sweep (recover, count), infected list, schedule, digit bases, bucket radix sort,
+ * bucket offsets, infection, apply.
  * days[0], days[1] receive the number of weekdays and weekend days timed.  The sums
  * reset after each call.  With timing enabled, a day run by pt_step_day or pt_run
  * records events but adds no host synchronisation. */
 pt_status pt_set_timing(pt_sim *sim, int enabled);
 pt_status pt_get_stage_ms(pt_sim *sim, float ms[16], int days[2]);
+
+/* The eight stage times of one day of the last timed run (zeros if that day was not
+ * timed).  The drop-in executable writes them as the reference's profile_log.csv. */
+pt_status pt_get_day_stage_ms(pt_sim *sim, int day, float ms[8]);
 
 /* Kernel launches issued by this library in the calling process so far. */
 uint64_t pt_launch_count(void);

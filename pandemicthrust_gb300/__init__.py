@@ -15,10 +15,10 @@ import os
 
 import numpy as np
 
-from .build import build as _build, LIB as LIBRARY_PATH, CLI as CLI_PATH
+from .build import build as _build, LIB as LIBRARY_PATH, CLI as CLI_PATH, BATCH_CLI as BATCH_CLI_PATH
 
 __all__ = ["PandemicSim", "PandemicBatch", "Params", "load_library", "build", "PtError", "LIBRARY_PATH",
-           "CLI_PATH", "PT_OK", "PT_DONE", "PT_FINISHED"]
+           "CLI_PATH", "BATCH_CLI_PATH", "PT_OK", "PT_DONE", "PT_FINISHED"]
 
 PT_OK, PT_DONE, PT_FINISHED = 0, 1, 2
 _STATUS = {0: "PT_OK", 1: "PT_DONE", 2: "PT_FINISHED", -1: "PT_ERR_ARG", -2: "PT_ERR_IO", -3: "PT_ERR_PARSE",
@@ -72,6 +72,7 @@ EXPORTS = [
     "pt_params_from_csv", "pt_seed_from_file", "pt_create", "pt_setup", "pt_step_day", "pt_run",
     "pt_final_gen_counts", "pt_reset_epidemic", "pt_get_info", "pt_get_person_state",
     "pt_get_population", "pt_get_day_tables", "pt_set_full_tables", "pt_set_timing", "pt_get_stage_ms",
+    "pt_get_day_stage_ms",
     "pt_launch_count", "pt_transfer_bytes", "pt_destroy", "pt_last_error",
     "pt_batch_create", "pt_batch_setup", "pt_batch_run", "pt_batch_step_day", "pt_batch_reset_epidemic",
     "pt_batch_size", "pt_batch_counts", "pt_batch_final_gen_counts", "pt_batch_get_info",
@@ -112,6 +113,7 @@ def load_library(path=None):
     lib.pt_set_timing.argtypes = [vp, ctypes.c_int]
     lib.pt_set_full_tables.argtypes = [vp, ctypes.c_int]
     lib.pt_get_stage_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ip]
+    lib.pt_get_day_stage_ms.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
     lib.pt_launch_count.restype = ctypes.c_uint64
     lib.pt_launch_count.argtypes = []
     lib.pt_transfer_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
@@ -238,7 +240,7 @@ class PandemicSim:
     def set_timing(self, on=True):
         self._check(self.lib.pt_set_timing(self.h, 1 if on else 0))
 
-    STAGES = ("sweep", "schedule", "bucket_scan", "bucket_sort", "infect", "apply")
+    STAGES = ("sweep", "infected_list", "schedule", "digit_bases", "bucket_sort", "bucket_offsets", "infect", "apply")
 
     def stage_ms(self):
         """Device ms per stage since the last call: ({weekday: {...}, weekend: {...}}, (weekdays, weekend days))."""

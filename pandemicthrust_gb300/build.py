@@ -4,7 +4,9 @@ Outputs, in-tree under pandemicthrust_gb300/_build/ (git-ignored):
   libpandemic_gb300.so   the C-ABI library declared in include/pandemic_gb300.h
   pt_sim                 drop-in executable: constants.csv + seed.txt in the working
                          directory -> output_infected_stats.csv, output_rn.csv,
-                         infected_max.txt (the reference's file contract)
+                         infected_max.txt, profile_log.csv (the reference's file contract)
+  pt_batch               batch driver: every experiment of a PythonBatcher
+                         experiment_files.txt (x seeds) as one batch
 Translation units compile in parallel; the whole build takes well under a minute.
 """
 import os
@@ -19,6 +21,7 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB = os.path.join(OUT, "libpandemic_gb300.so")
 CLI = os.path.join(OUT, "pt_sim")
+BATCH_CLI = os.path.join(OUT, "pt_batch")
 
 CUDA_SOURCES = ["pt_kernels.cu", "pt_static_table.cu"]
 HOST_SOURCES = ["pt_sim.cpp", "pt_host.cpp"]
@@ -38,8 +41,9 @@ def _sources_mtime():
 
 def build(verbose=False, force=False):
     os.makedirs(OUT, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.exists(CLI) and \
-            min(os.path.getmtime(LIB), os.path.getmtime(CLI)) >= _sources_mtime():
+    outputs = (LIB, CLI, BATCH_CLI)
+    if not force and all(os.path.exists(f) for f in outputs) and \
+            min(os.path.getmtime(f) for f in outputs) >= _sources_mtime():
         return LIB
     nvcc = _nvcc()
     common = ["-std=c++17", "-O3", "-I", INCLUDE, "-I", CSRC, "-Xcompiler", "-fPIC"]
@@ -68,11 +72,20 @@ def build(verbose=False, force=False):
     if verbose:
         print(" ".join(link))
     subprocess.check_call(link)
-    cli_obj = os.path.join(OUT, "pt_cli.cpp.o")
-    subprocess.check_call([nvcc] + common + ["-Xcompiler", "-ffp-contract=off", "-c",
-                                             os.path.join(CSRC, "pt_cli.cpp"), "-o", cli_obj])
-    subprocess.check_call([nvcc] + ARCH + ["-o", CLI, cli_obj, "-L", OUT, "-lpandemic_gb300",
-                                           "-Xlinker", "-rpath,$ORIGIN"])
+    # the executables: the drop-in pt_sim and the batch driver, both over the library
+    cli_objs = {}
+    procs = []
+    for src in ("pt_cli.cpp", "pt_batch_cli.cpp", "pt_output.cpp"):
+        obj = os.path.join(OUT, src + ".o")
+        cli_objs[src] = obj
+        procs.append(subprocess.Popen([nvcc] + common + ["-Xcompiler", "-ffp-contract=off", "-c",
+                                                         os.path.join(CSRC, src), "-o", obj]))
+    bad = [p.args for p in procs if p.wait() != 0]
+    if bad:
+        raise RuntimeError("compile failed: %s" % bad[0])
+    for exe, main_src in ((CLI, "pt_cli.cpp"), (BATCH_CLI, "pt_batch_cli.cpp")):
+        subprocess.check_call([nvcc] + ARCH + ["-o", exe, cli_objs[main_src], cli_objs["pt_output.cpp"], "-L", OUT,
+                                               "-lpandemic_gb300", "-Xlinker", "-rpath,$ORIGIN"])
     return LIB
 
 

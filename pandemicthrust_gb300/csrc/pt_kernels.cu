@@ -962,6 +962,12 @@ cudaError_t launch_sweep(const DevArrays &d, int day, cudaStream_t s)
     count_launch();
     k_sweep_scan<<<1, kSweepScanThreads, 0, s>>>(d.ic, d.is, d.K, d.sweep_tiles, tiles, d.sc, day);
     count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_infected_list(const DevArrays &d, cudaStream_t s)
+{
+    const int tiles = d.P / kSweepTile;
     k_sweep_emit<<<tiles, kSweepThreads, 0, s>>>(d.tile_inst, d.sweep_flags, d.sweep_tiles, d.infected,
                                                  d.infected_inst, d.sc);
     count_launch();
@@ -1401,11 +1407,14 @@ __global__ void k_bucket_offsets(const uint32_t *keys, RadixSegments sg, int wee
     }
 }
 
-cudaError_t launch_bucket_sort(const DevArrays &d, bool weekend, bool full_tables, cudaStream_t s)
+cudaError_t launch_bucket_sort(const DevArrays &d, bool weekend, cudaStream_t s)
+{
+    return launch_radix_sort(day_radix_args(d, weekend), s);
+}
+
+cudaError_t launch_bucket_offsets(const DevArrays &d, bool weekend, bool full_tables, cudaStream_t s)
 {
     const RadixArgs r = day_radix_args(d, weekend);
-    cudaError_t e = launch_radix_sort(r, s);
-    if (e != cudaSuccess) return e;
     const int P = radix_passes(r.buckets);
     const uint32_t *sorted = ((P - 1) & 1) ? r.k1 : r.k0;  // where the last pass wrote the keys
     k_bucket_offsets<<<sm_count() * 8, 256, 0, s>>>(sorted, r.seg, weekend ? 1 : 0, full_tables ? 1 : 0,

@@ -177,10 +177,12 @@ cudaError_t launch_seed_infected(const int32_t *seeds, int P, int S, uint32_t *s
                                  uint8_t *gen_s, cudaStream_t s);
 
 // ---- day (every instance of the batch in each launch)
-cudaError_t launch_sweep(const DevArrays &d, int day, cudaStream_t s);
+cudaError_t launch_sweep(const DevArrays &d, int day, cudaStream_t s);          // recover, count, scan, bookkeeping
+cudaError_t launch_infected_list(const DevArrays &d, cudaStream_t s);           // the ordered infected list
 cudaError_t launch_schedule(const DevArrays &d, bool weekend, int day, bool full_tables, cudaStream_t s);
 cudaError_t launch_bucket_scan(const DevArrays &d, bool weekend, cudaStream_t s);
-cudaError_t launch_bucket_sort(const DevArrays &d, bool weekend, bool full_tables, cudaStream_t s);
+cudaError_t launch_bucket_sort(const DevArrays &d, bool weekend, cudaStream_t s);
+cudaError_t launch_bucket_offsets(const DevArrays &d, bool weekend, bool full_tables, cudaStream_t s);
 cudaError_t launch_infect(const DevArrays &d, bool weekend, int day, cudaStream_t s);
 cudaError_t launch_apply(const DevArrays &d, int day, cudaStream_t s);
 // weekday / weekend buckets of one instance (compact keys hour * R + dest - lo)

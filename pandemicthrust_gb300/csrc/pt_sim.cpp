@@ -57,7 +57,8 @@ struct Instance {
 };
 
 // Stage boundaries recorded per day when timing is on.
-enum { kStSweep, kStSchedule, kStScan, kStRadix, kStInfect, kStApply, kStages };
+enum { kStSweep, kStInfectedList, kStSchedule, kStDigits, kStRadix, kStOffsets, kStInfect, kStApply, kStages };
+static_assert(kStages == 8, "eight stages per day type in pt_get_stage_ms");
 
 }  // namespace
 
@@ -87,6 +88,7 @@ struct Engine {
     std::vector<int> timed_days;
     float stage_ms[16] = {0};             // [weekday stages 0..7, weekend stages 8..15]
     int stage_days[2] = {0, 0};
+    std::vector<float> day_stage_ms;      // kMaxDays x kStages: the last timed run of each day
     mutable uint64_t h2d_bytes = 0, d2h_bytes = 0;  // host<->device copies issued
     // The whole day loop (days 0..max_days-1) captured once and replayed by run().
     // Every per-day decision (early stop, counters, offsets) reads device state, so
@@ -475,19 +477,23 @@ static pt_status enqueue_day(Engine *s, int day)
     const ptk::DevArrays &d = s->d;
     cudaStream_t st = s->stream;
     const bool t = s->timing;
-    if (t) cudaEventRecord(stage_event(s, day, 0), st);
+    if (t) cudaEventRecord(stage_event(s, day, kStSweep), st);
     CK(ptk::launch_sweep(d, day, st), "sweep");
-    if (t) cudaEventRecord(stage_event(s, day, 1), st);
+    if (t) cudaEventRecord(stage_event(s, day, kStInfectedList), st);
+    CK(ptk::launch_infected_list(d, st), "infected list");
+    if (t) cudaEventRecord(stage_event(s, day, kStSchedule), st);
     CK(ptk::launch_schedule(d, weekend, day, s->full_tables, st), "schedule");
-    if (t) cudaEventRecord(stage_event(s, day, 2), st);
-    CK(ptk::launch_bucket_scan(d, weekend, st), "bucket scan");
-    if (t) cudaEventRecord(stage_event(s, day, 3), st);
-    CK(ptk::launch_bucket_sort(d, weekend, s->full_tables, st), "bucket sort");
-    if (t) cudaEventRecord(stage_event(s, day, 4), st);
+    if (t) cudaEventRecord(stage_event(s, day, kStDigits), st);
+    CK(ptk::launch_bucket_scan(d, weekend, st), "digit bases");
+    if (t) cudaEventRecord(stage_event(s, day, kStRadix), st);
+    CK(ptk::launch_bucket_sort(d, weekend, st), "bucket sort");
+    if (t) cudaEventRecord(stage_event(s, day, kStOffsets), st);
+    CK(ptk::launch_bucket_offsets(d, weekend, s->full_tables, st), "bucket offsets");
+    if (t) cudaEventRecord(stage_event(s, day, kStInfect), st);
     CK(ptk::launch_infect(d, weekend, day, st), "infect");
-    if (t) cudaEventRecord(stage_event(s, day, 5), st);
+    if (t) cudaEventRecord(stage_event(s, day, kStApply), st);
     CK(ptk::launch_apply(d, day, st), "apply");
-    if (t) cudaEventRecord(stage_event(s, day, 6), st);
+    if (t) cudaEventRecord(stage_event(s, day, kStages), st);
     if (t) s->timed_days.push_back(day);
     return PT_OK;
 }
@@ -498,10 +504,12 @@ static void accumulate_timing(Engine *s)
     cudaStreamSynchronize(s->stream);
     for (int day : s->timed_days) {
         const bool weekend = (day % 7) >= 5;
+        if (s->day_stage_ms.empty()) s->day_stage_ms.assign((size_t)ptk::kMaxDays * kStages, 0.f);
         for (int k = 0; k < kStages; k++) {
             float ms = 0.f;
             if (cudaEventElapsedTime(&ms, stage_event(s, day, k), stage_event(s, day, k + 1)) == cudaSuccess)
                 s->stage_ms[(weekend ? 8 : 0) + k] += ms;
+            s->day_stage_ms[(size_t)day * kStages + k] = ms;
         }
         s->stage_days[weekend ? 1 : 0]++;
     }
@@ -922,6 +930,15 @@ pt_status pt_get_stage_ms(pt_sim *s, float ms[16], int days[2])
 {
     if (!s || !ms) return PT_ERR_ARG;
     return engine_stage_ms(s, ms, days);
+}
+
+pt_status pt_get_day_stage_ms(pt_sim *s, int day, float ms[8])
+{
+    if (!s || !ms || day < 0 || day >= ptk::kMaxDays) return PT_ERR_ARG;
+    accumulate_timing(s);
+    for (int k = 0; k < kStages; k++)
+        ms[k] = s->day_stage_ms.empty() ? 0.f : s->day_stage_ms[(size_t)day * kStages + k];
+    return PT_OK;
 }
 
 uint64_t pt_launch_count(void) { return ptk::launches(); }

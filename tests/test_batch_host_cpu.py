@@ -43,3 +43,17 @@ def test_batch_instances_derive_like_standalone(native_lib):
         assert np.array(bi["infectiousness"], np.float32).tobytes() == np.array(si["infectiousness"], np.float32).tobytes()
         sim.close()
     b.close()
+
+
+def test_batch_driver_rejects_bad_arguments_before_any_device_work(native_lib, tmp_path):
+    import subprocess
+    proc = subprocess.run([pt.BATCH_CLI_PATH, "--list", str(tmp_path / "missing.txt")], cwd=str(tmp_path),
+                          capture_output=True, text=True, timeout=60)
+    assert proc.returncode == 1 and "missing.txt" in proc.stderr
+    proc = subprocess.run([pt.BATCH_CLI_PATH, "--seeds", "1,,2"], cwd=str(tmp_path), capture_output=True, text=True,
+                          timeout=60)
+    assert proc.returncode == 2
+    (tmp_path / "empty.txt").write_text("\n")
+    proc = subprocess.run([pt.BATCH_CLI_PATH, "--list", str(tmp_path / "empty.txt")], cwd=str(tmp_path),
+                          capture_output=True, text=True, timeout=60)
+    assert proc.returncode == 1 and "no experiments" in proc.stderr
