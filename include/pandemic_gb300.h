@@ -70,6 +70,26 @@ typedef struct pt_info {
     uint64_t bucket_entries_materialised; /* of those, entries written to bucket tables */
 } pt_info;
 
+/* Public-health interventions.  The reference has none (its thesis, section 6.1,
+ * only sketches them); these are this library's extensions, and all fields zero
+ * reproduce the reference exactly.  Their random choices use a hash of (seed, day,
+ * person), never the reference's random stream.
+ *   school closure: on days [start, start + days) workplace / school contacts made at
+ *     school-type locations (types 3-7) do not happen;
+ *   workplace absenteeism: on each weekday each adult is absent from work with this
+ *     probability; workplace / school contacts of an absent infector, or with an
+ *     absent adult, do not happen;
+ *   vaccination coverage: this fraction of persons starts recovered from both
+ *     strains (initial infections are placed afterwards, as in the reference).
+ * A contact that does not happen keeps its weight in the infector's contact sum, so
+ * it removes transmission instead of moving it to the other contacts. */
+typedef struct pt_interventions {
+    int   school_closure_start;   /* first closed day, >= 0 */
+    int   school_closure_days;    /* 0: schools stay open */
+    float workplace_absenteeism;  /* 0..1 */
+    float vaccination_coverage;   /* 0..1 */
+} pt_interventions;
+
 typedef struct pt_sim pt_sim;
 
 /* PandemicSim::setup_loadParameters (PandemicSim.cu:286-310): the reference's
@@ -135,6 +155,11 @@ pt_status pt_get_population(pt_sim *sim, int32_t *household, int32_t *household_
  * pt_set_full_tables(sim, 1). */
 pt_status pt_get_day_tables(pt_sim *sim, int32_t *infected, int32_t *keys, int32_t *people,
                             int32_t *offsets, int *entries, int *buckets);
+
+/* Sets the simulation's interventions (see pt_interventions; no counterpart in the
+ * reference).  Allowed before or after pt_setup; vaccination takes effect at setup or
+ * at the next pt_reset_epidemic, the others from the next day run. */
+pt_status pt_set_interventions(pt_sim *sim, const pt_interventions *iv);
 
 /* With enabled != 0 every day materialises all of its buckets, not only those its
  * infected persons visit.  Results are identical either way; this exists so the
@@ -220,6 +245,9 @@ pt_status pt_batch_run(pt_batch *batch);
 pt_status pt_batch_step_day(pt_batch *batch, int *running);
 
 pt_status pt_batch_reset_epidemic(pt_batch *batch);
+
+/* pt_set_interventions for every instance: iv holds one entry per instance. */
+pt_status pt_batch_set_interventions(pt_batch *batch, const pt_interventions *iv);
 
 /* Instance count, real persons over all instances and persons including the padding
  * that starts each instance on a 4096-person boundary. */

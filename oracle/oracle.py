@@ -169,6 +169,8 @@ def oracle_lib():
         lib.ptor_glibc_srand.argtypes = [ctypes.c_void_p, ctypes.c_uint]
         lib.ptor_glibc_rand_next.argtypes = [ctypes.c_void_p]
         lib.ptor_set_threads.argtypes = [ctypes.c_int]
+        lib.ptor_set_interventions.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                               ctypes.c_float]
         _oracle_lib = lib
     return _oracle_lib
 
@@ -209,6 +211,12 @@ class Oracle:
         self.h = self.lib.ptor_create(ctypes.byref(self._p), seed)
         if not self.h:
             raise ValueError("oracle rejected the parameters")
+
+    def set_interventions(self, school_closure_start=0, school_closure_days=0, workplace_absenteeism=0.0,
+                          vaccination_coverage=0.0):
+        """The build's intervention extensions (no reference counterpart); before setup()."""
+        self.lib.ptor_set_interventions(self.h, int(school_closure_start), int(school_closure_days),
+                                        float(workplace_absenteeism), float(vaccination_coverage))
 
     def setup(self):
         rc = self.lib.ptor_setup(self.h)

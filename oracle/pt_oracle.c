@@ -212,7 +212,44 @@ struct ptor_sim {
     int32_t *ecursor;
     int e_entries, e_buckets;
     int setup_done;
+    /* interventions (the build's extensions; all zero reproduces the reference) */
+    int closure_start, closure_end;
+    uint64_t absent_thr, vacc_thr;
 };
+
+/* Interventions have no counterpart in the reference.  Their random choices use the
+ * splitmix64 finaliser (Steele, Lea and Flood, OOPSLA 2014) over (key, tag, day,
+ * person), apart from the reference's Threefry stream: high 32 bits of
+ * mix(mix(key0 ^ (key1 << 1) ^ tag) ^ (day << 32 | person)). */
+enum { TAG_ABSENT = 1, TAG_VACCINATED = 2 };
+
+static uint64_t splitmix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static uint64_t intervention_hash(const ptor_sim *s, uint64_t tag, int day, int person)
+{
+    uint64_t k = splitmix64(s->key[0] ^ (s->key[1] << 1) ^ tag);
+    return splitmix64(k ^ (((uint64_t)(uint32_t)day << 32) | (uint32_t)person)) >> 32;
+}
+
+static uint64_t fraction_threshold(float f)
+{
+    double t = (double)f * 4294967296.0;
+    return t <= 0.0 ? 0ull : (t >= 4294967296.0 ? 4294967296ull : (uint64_t)(t + 0.5));
+}
+
+void ptor_set_interventions(ptor_sim *s, int closure_start, int closure_days, float absenteeism, float coverage)
+{
+    s->closure_start = closure_start;
+    s->closure_end = closure_days > 0 ? closure_start + closure_days : 0;
+    s->absent_thr = fraction_threshold(absenteeism);
+    s->vacc_thr = fraction_threshold(coverage);
+}
 
 static int g_threads = 0;
 void ptor_set_threads(int n) { g_threads = n; }
@@ -563,6 +600,13 @@ int ptor_setup(ptor_sim *s)
     memset(s->day_s, DAY_NOT_INFECTED, n);
     memset(s->gen_p, GEN_NOT_INFECTED, n);
     memset(s->gen_s, GEN_NOT_INFECTED, n);
+    /* vaccination (intervention): recovered from both strains, never infected */
+    if (s->vacc_thr)
+        for (int i = 0; i < N; i++)
+            if (intervention_hash(s, TAG_VACCINATED, 0, i) < s->vacc_thr) {
+                s->status_p[i] = STATUS_RECOVERED;
+                s->status_s[i] = STATUS_RECOVERED;
+            }
 
     /* setup_initialInfected + n_unique_numbers, PandemicSim.cu:708-758, :1642-1659:
      * distinct rand() % N, the first P pandemic, the next S seasonal; status
@@ -732,7 +776,8 @@ static float infection_probability(const ptor_sim *s, int profile, int pday, int
 }
 
 /* device_makeContacts_weekday, PandemicSim.cu:1669-1829 */
-static int make_contacts_weekday(const ptor_sim *s, int me, uint64_t c, int victims[8], int types[8])
+static int make_contacts_weekday(const ptor_sim *s, int me, uint64_t c, int victims[8], int types[8],
+                                 int *work_slots, int *work_loc)
 {
     uint32_t w[8];
     tf_words(s, c, w);
@@ -749,6 +794,8 @@ static int make_contacts_weekday(const ptor_sim *s, int me, uint64_t c, int vict
     int desired = workplace_max_contacts(s, wp);
     int ctype = (age == AGE_ADULT) ? CONTACT_WORKPLACE : CONTACT_SCHOOL;
     int local = made;
+    *work_slots = desired;
+    *work_loc = wp;
     made += desired;
     while (desired > 0) {
         ksum += select_victim(me, woff, wcnt, w[local], ctype, s->wp_people, &victims[local], &types[local]);
@@ -868,8 +915,27 @@ void ptor_infect(ptor_sim *s)
             ksum = make_contacts_weekend(s, me, c, victims, types);
             nc = MAX_CONTACTS_WEEKEND;
         } else {
-            ksum = make_contacts_weekday(s, me, c, victims, types);
+            int wslots = 0, wloc = 0;
+            ksum = make_contacts_weekday(s, me, c, victims, types, &wslots, &wloc);
             nc = MAX_CONTACTS_WEEKDAY;
+            /* interventions: a closed school or an absent adult voids the workplace /
+             * school contacts, which keep their share of ksum */
+            int day = s->day;
+            int closed_day = day >= s->closure_start && day < s->closure_end;
+            if (wslots > 0 && (s->absent_thr || closed_day)) {
+                int lid = wloc % s->L;
+                int school = lid >= s->type_offset[3] && lid < s->type_offset[7] + s->type_count[7];
+                int closed = closed_day && school;
+                int me_absent = s->age[me] == AGE_ADULT && s->absent_thr &&
+                                intervention_hash(s, TAG_ABSENT, day, me) < s->absent_thr;
+                for (int j = 3; j < 3 + wslots; j++) {
+                    if (KVAL[types[j]] == 0) continue;
+                    int v = victims[j];
+                    int v_absent = s->absent_thr && s->age[v] == AGE_ADULT &&
+                                   intervention_hash(s, TAG_ABSENT, day, v) < s->absent_thr;
+                    if (closed || me_absent || v_absent) types[j] = CONTACT_NONE;
+                }
+            }
         }
         process_contacts(s, me, ksum, victims, types, nc, c + 2);
     }

@@ -104,6 +104,8 @@ int  ptor_recalc_weekday_errands(const ptor_sim *s, uint64_t errand_offset, int 
                                  int *dest1, int *dest2);
 void ptor_recalc_weekend_errands(const ptor_sim *s, uint64_t errand_offset, int idx, int dests[3]);
 void ptor_set_threads(int n);
+/* Interventions (the build's extensions, no reference counterpart); before setup. */
+void ptor_set_interventions(ptor_sim *s, int closure_start, int closure_days, float absenteeism, float coverage);
 
 #ifdef __cplusplus
 }

@@ -17,7 +17,7 @@ import numpy as np
 
 from .build import build as _build, LIB as LIBRARY_PATH, CLI as CLI_PATH, BATCH_CLI as BATCH_CLI_PATH
 
-__all__ = ["PandemicSim", "PandemicBatch", "Params", "load_library", "build", "PtError", "LIBRARY_PATH",
+__all__ = ["PandemicSim", "PandemicBatch", "Params", "Interventions", "load_library", "build", "PtError", "LIBRARY_PATH",
            "CLI_PATH", "BATCH_CLI_PATH", "PT_OK", "PT_DONE", "PT_FINISHED"]
 
 PT_OK, PT_DONE, PT_FINISHED = 0, 1, 2
@@ -53,6 +53,24 @@ class Params(ctypes.Structure):
         return p
 
 
+class Interventions(ctypes.Structure):
+    """pt_interventions: the build's extensions (no reference counterpart); all zero
+    reproduces the reference."""
+    _fields_ = [
+        ("school_closure_start", ctypes.c_int),
+        ("school_closure_days", ctypes.c_int),
+        ("workplace_absenteeism", ctypes.c_float),
+        ("vaccination_coverage", ctypes.c_float),
+    ]
+
+    @classmethod
+    def from_dict(cls, d):
+        iv = cls()
+        for name, _ in cls._fields_:
+            setattr(iv, name, d.get(name, 0))
+        return iv
+
+
 class Info(ctypes.Structure):
     _fields_ = [
         ("number_people", ctypes.c_int), ("number_households", ctypes.c_int),
@@ -72,7 +90,7 @@ EXPORTS = [
     "pt_params_from_csv", "pt_seed_from_file", "pt_create", "pt_setup", "pt_step_day", "pt_run",
     "pt_final_gen_counts", "pt_reset_epidemic", "pt_get_info", "pt_get_person_state",
     "pt_get_population", "pt_get_day_tables", "pt_set_full_tables", "pt_set_timing", "pt_get_stage_ms",
-    "pt_get_day_stage_ms",
+    "pt_get_day_stage_ms", "pt_set_interventions", "pt_batch_set_interventions",
     "pt_launch_count", "pt_transfer_bytes", "pt_destroy", "pt_last_error",
     "pt_batch_create", "pt_batch_setup", "pt_batch_run", "pt_batch_step_day", "pt_batch_reset_epidemic",
     "pt_batch_size", "pt_batch_counts", "pt_batch_final_gen_counts", "pt_batch_get_info",
@@ -114,6 +132,8 @@ def load_library(path=None):
     lib.pt_set_full_tables.argtypes = [vp, ctypes.c_int]
     lib.pt_get_stage_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ip]
     lib.pt_get_day_stage_ms.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+    lib.pt_set_interventions.argtypes = [vp, ctypes.POINTER(Interventions)]
+    lib.pt_batch_set_interventions.argtypes = [vp, ctypes.POINTER(Interventions)]
     lib.pt_launch_count.restype = ctypes.c_uint64
     lib.pt_launch_count.argtypes = []
     lib.pt_transfer_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
@@ -233,6 +253,12 @@ class PandemicSim:
         return dict(infected=infected, keys=keys[:e.value], people=people[:e.value],
                     offsets=offsets[:b.value + 1], entries=e.value, buckets=b.value)
 
+    def set_interventions(self, iv):
+        """School closure, workplace absenteeism, vaccination (a dict or Interventions)."""
+        if isinstance(iv, dict):
+            iv = Interventions.from_dict(iv)
+        self._check(self.lib.pt_set_interventions(self.h, ctypes.byref(iv)))
+
     def set_full_tables(self, on=True):
         """Materialise every bucket each day (complete tables for day_tables())."""
         self._check(self.lib.pt_set_full_tables(self.h, 1 if on else 0))
@@ -324,6 +350,11 @@ class PandemicBatch:
 
     def reset_epidemic(self):
         self._check(self.lib.pt_batch_reset_epidemic(self.h))
+
+    def set_interventions(self, ivs):
+        """One intervention dict (or Interventions) per instance."""
+        arr = (Interventions * self.k)(*[Interventions.from_dict(i) if isinstance(i, dict) else i for i in ivs])
+        self._check(self.lib.pt_batch_set_interventions(self.h, arr))
 
     def size(self):
         """(instances, persons, persons including padding)."""

@@ -239,6 +239,34 @@ __device__ __forceinline__ void weekend_errands(const SimConst &c, const TfKey &
     out[2] = fish_weekend_dest(c, w[5]) - lo + h3 * R;
 }
 
+// ---------------------------------------------------------------- interventions
+// The interventions have no counterpart in the reference.  Their random choices come
+// from this hash, not from the reference's Threefry counter stream, so a run whose
+// interventions are all zero draws exactly the reference's numbers.  The mix is the
+// splitmix64 finaliser (Steele, Lea and Flood, OOPSLA 2014); the high 32 bits of
+// mix(mix(key0 ^ (key1 << 1) ^ tag) ^ (day << 32 | person)) decide.
+__host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__host__ __device__ __forceinline__ uint64_t intervention_hash(uint64_t key0, uint64_t key1, uint64_t tag, int day,
+                                                               int person)
+{
+    const uint64_t k = splitmix64(key0 ^ (key1 << 1) ^ tag);
+    return splitmix64(k ^ (((uint64_t)(uint32_t)day << 32) | (uint32_t)person)) >> 32;
+}
+
+// School-type locations: types 3-7 (the children's schools by age band,
+// PandemicSim.cu:2402-2442), contiguous in location order.
+__device__ __forceinline__ bool is_school(const SimConst &c, int loc)
+{
+    return loc >= c.type_offset[3] && loc < c.type_offset[7] + c.type_count[7];
+}
+
 // device_getWorkplaceMaxContacts, PandemicSim.cu:3492-3511
 __device__ __forceinline__ int workplace_max_contacts(const SimConst &c, int loc)
 {

@@ -654,6 +654,29 @@ cudaError_t launch_reset_instances(const DevArrays &d, cudaStream_t s)
     return cudaGetLastError();
 }
 
+// Vaccination (an intervention, no reference counterpart): one person tile per block;
+// a vaccinated person starts recovered from both strains, never infected.
+__global__ void k_vaccinate(const InstConst *ic, const int32_t *tile_inst, uint32_t *state)
+{
+    const int k = tile_inst[blockIdx.x];
+    const InstConst &c = ic[k];
+    if (c.vacc_thr == 0) return;
+    const int first = blockIdx.x * kPersonTile - c.pbase;
+    for (int i = threadIdx.x; i < kPersonTile; i += blockDim.x) {
+        const int p = first + i;
+        if (p >= c.c.N) break;
+        if (intervention_hash(c.c.key0, c.c.key1, kTagVaccinated, 0, p) < c.vacc_thr)
+            state[c.pbase + p] = (0xFFu << 16) | (0xFFu << 24);  // status R / R, day 255 / 255
+    }
+}
+
+cudaError_t launch_vaccinate(const DevArrays &d, cudaStream_t s)
+{
+    k_vaccinate<<<d.P / kPersonTile, 256, 0, s>>>(d.ic, d.tile_inst, d.state);
+    count_launch();
+    return cudaGetLastError();
+}
+
 // setup_initialInfected (PandemicSim.cu:708-758): the first P seeds get the pandemic
 // strain, the next S the seasonal one; status STATUS_INFECTED, day 0, generation 0.
 __global__ void k_seed_infected(const int32_t *seeds, int P, int S, uint32_t *state, uint8_t *gen_p, uint8_t *gen_s)
@@ -1569,6 +1592,7 @@ __global__ void __launch_bounds__(128) k_infect_weekday(InfectArgs a, int day)
             prof = (int)((e[slot] ^ e[slot + 1]) % 3u);
         }
         int made = 3;
+        uint32_t wvoid = 0;  // contact slots voided by interventions
 #pragma unroll
         for (int j = 3; j < 8; j++) {
             victims[j] = -1;
@@ -1582,6 +1606,24 @@ __global__ void __launch_bounds__(128) k_infect_weekday(InfectArgs a, int day)
             }
         }
         made += desired;
+        // interventions: a closed school or an absent adult voids the workplace / school
+        // contacts; they keep their share of ksum, so the contact does not happen
+        // rather than passing its weight to the others
+        if (desired > 0 && (ik.absent_thr != 0 || (day >= ik.closure_start && day < ik.closure_end))) {
+            const bool closed = day >= ik.closure_start && day < ik.closure_end && is_school(c, wp - ik.lbase);
+            const bool me_absent =
+                adult && intervention_hash(c.key0, c.key1, kTagAbsent, day, lme) < ik.absent_thr;
+#pragma unroll
+            for (int j = 3; j < 6; j++) {
+                if (j - 3 < desired && kv[j] != 0) {
+                    const int v = victims[j];
+                    const bool v_absent = ik.absent_thr != 0 && a.age[v] == 5 &&
+                                          intervention_hash(c.key0, c.key1, kTagAbsent, day, v - ik.pbase) <
+                                              ik.absent_thr;
+                    if (closed || me_absent || v_absent) wvoid |= 1u << j;
+                }
+            }
+        }
 #pragma unroll
         for (int hour = 0; hour < 2; hour++) {
             int want = c_weekday_assign[prof][hour];
@@ -1597,6 +1639,9 @@ __global__ void __launch_bounds__(128) k_infect_weekday(InfectArgs a, int day)
             }
         }
         infector_state(c, inf, a.state[me], a.gen_p, a.gen_s, day, ksum);
+#pragma unroll
+        for (int j = 3; j < 6; j++)
+            if ((wvoid >> j) & 1u) kv[j] = 0;
         process_contacts<8>(c, key, inf, ctr + 2, victims, kv, a.state, a.claim, a.new_list, sc);
     }
 }

@@ -42,7 +42,13 @@ struct InstConst {
                            // slot follows them (the end offset of its last bucket)
     int max_days;
     long long kbase;       // first schedule-key slot (3 * pbase)
+    // interventions (build-defined extensions; all zero reproduces the reference)
+    int closure_start, closure_end;  // school-type locations closed on days [start, end)
+    uint64_t absent_thr;             // an adult is absent from work when intervention_hash < this
+    uint64_t vacc_thr;               // a person starts vaccinated when intervention_hash < this
 };
+
+constexpr uint64_t kTagAbsent = 1, kTagVaccinated = 2;
 
 // Device-resident state of one simulation.  The day loop reads and updates it on
 // the device, so a whole run needs no host round trip.
@@ -173,6 +179,9 @@ cudaError_t launch_init_status(int N, uint32_t *state, uint8_t *gen_p, uint8_t *
 // every instance's device state back to "set up, day 0": rand_offset after setup is
 // H/4 (household types) + N/4 (workplaces)
 cudaError_t launch_reset_instances(const DevArrays &d, cudaStream_t s);
+// vaccinated persons start recovered from both strains (only when some instance
+// has a vaccination coverage)
+cudaError_t launch_vaccinate(const DevArrays &d, cudaStream_t s);
 cudaError_t launch_seed_infected(const int32_t *seeds, int P, int S, uint32_t *state, uint8_t *gen_p,
                                  uint8_t *gen_s, cudaStream_t s);
 

@@ -47,6 +47,7 @@ struct Instance {
     std::vector<int32_t> seed_list;   // the instance's person numbers
     ptk::SimConst c;
     int adults = 0;
+    pt_interventions iv{};            // all zero: the reference's model
     int day = 0;                      // next day to run
     bool stopped = false;             // a day counted zero infected
     int days_run = 0;
@@ -193,6 +194,47 @@ static pt_status engine_create(Engine *s, const pt_params *params, const int *co
 
 static pt_status engine_reset(Engine *s);
 
+// A fraction in [0, 1] as a threshold on a 32-bit hash value: hash < threshold with
+// probability `fraction`.
+static uint64_t fraction_threshold(float fraction)
+{
+    const double t = (double)fraction * 4294967296.0;
+    return t <= 0.0 ? 0ull : (t >= 4294967296.0 ? 4294967296ull : (uint64_t)(t + 0.5));
+}
+
+static void apply_interventions(ptk::InstConst &r, const pt_interventions &iv)
+{
+    r.closure_start = iv.school_closure_start;
+    r.closure_end = iv.school_closure_days > 0 ? iv.school_closure_start + iv.school_closure_days : 0;
+    r.absent_thr = fraction_threshold(iv.workplace_absenteeism);
+    r.vacc_thr = fraction_threshold(iv.vaccination_coverage);
+}
+
+static const char *check_interventions(const pt_interventions &iv)
+{
+    if (iv.school_closure_start < 0 || iv.school_closure_days < 0 || iv.school_closure_days > 256)
+        return "school closure start and days must be >= 0 (days <= 256)";
+    if (!(iv.workplace_absenteeism >= 0.f && iv.workplace_absenteeism <= 1.f))
+        return "workplace absenteeism must be in [0, 1]";
+    if (!(iv.vaccination_coverage >= 0.f && iv.vaccination_coverage <= 1.f))
+        return "vaccination coverage must be in [0, 1]";
+    return nullptr;
+}
+
+// Sets instance k's interventions; after setup the device record is updated at once
+// (vaccination takes effect at the next reset).
+static pt_status engine_set_interventions(Engine *s, int k, const pt_interventions &iv)
+{
+    if (const char *why = check_interventions(iv)) return fail(s, PT_ERR_ARG, why);
+    s->inst[k].iv = iv;
+    if (s->setup_done) {
+        apply_interventions(s->ic[k], iv);
+        CK(pt_memcpy_sync(s, (void *)(s->d.ic + k), &s->ic[k], sizeof(ptk::InstConst), cudaMemcpyHostToDevice),
+           "instance record");
+    }
+    return PT_OK;
+}
+
 // PandemicSim::setupSim (PandemicSim.cu:146-208) for every instance: population,
 // households, workplaces and schools, the workplace table, status arrays, initial
 // infected.  Household types and workplace draws run per instance (each has its own
@@ -301,6 +343,7 @@ static pt_status engine_setup(Engine *s)
         d.bucket_max[1] = std::max(d.bucket_max[1], r.bcount[1]);
         r.max_days = s->inst[k].params.max_days;
         r.kbase = 3ll * pbase[k];
+        apply_interventions(r, s->inst[k].iv);
     }
     CK(pt_memcpy(s, ic_dev, s->ic.data(), (size_t)K * sizeof(ptk::InstConst), cudaMemcpyHostToDevice, s->stream),
        "instance records");
@@ -442,6 +485,9 @@ static pt_status engine_reset(Engine *s)
 {
     ptk::DevArrays &d = s->d;
     CK(ptk::launch_init_status(d.P, d.state, d.gen_p, d.gen_s, d.claim, s->stream), "init_status");
+    bool vaccination = false;
+    for (const ptk::InstConst &r : s->ic) vaccination |= r.vacc_thr != 0;
+    if (vaccination) CK(ptk::launch_vaccinate(d, s->stream), "vaccinate");
     if (!s->seed_global.empty()) {
         CK(pt_memcpy(s, s->d_seeds, s->seed_global.data(), sizeof(int32_t) * s->seed_global.size(),
                      cudaMemcpyHostToDevice, s->stream), "seed copy");
@@ -907,6 +953,12 @@ pt_status pt_get_day_tables(pt_sim *s, int32_t *infected, int32_t *keys, int32_t
     return PT_OK;
 }
 
+pt_status pt_set_interventions(pt_sim *s, const pt_interventions *iv)
+{
+    if (!s || !iv) return PT_ERR_ARG;
+    return engine_set_interventions(s, 0, *iv);
+}
+
 pt_status pt_set_full_tables(pt_sim *s, int enabled)
 {
     if (!s) return PT_ERR_ARG;
@@ -997,6 +1049,19 @@ pt_status pt_batch_reset_epidemic(pt_batch *b)
     if (!b) return PT_ERR_ARG;
     if (!b->setup_done) return fail(b, PT_ERR_STATE, "reset before setup");
     return engine_reset(b);
+}
+
+pt_status pt_batch_set_interventions(pt_batch *b, const pt_interventions *iv)
+{
+    if (!b || !iv) return PT_ERR_ARG;
+    for (int k = 0; k < b->K(); k++)
+        if (const char *why = check_interventions(iv[k]))
+            return fail(b, PT_ERR_ARG, "instance " + std::to_string(k) + ": " + why);
+    for (int k = 0; k < b->K(); k++) {
+        pt_status st = engine_set_interventions(b, k, iv[k]);
+        if (st != PT_OK) return st;
+    }
+    return PT_OK;
 }
 
 pt_status pt_batch_size(const pt_batch *b, int *instances, int64_t *persons, int64_t *padded_persons)
