@@ -211,6 +211,31 @@ pt_status pt_transfer_bytes(const pt_sim *sim, uint64_t *h2d, uint64_t *d2h);
 pt_status pt_bucket_table_static(const int32_t *keys, int n, int buckets, int32_t *offsets,
                                  int32_t *table, void *cuda_stream);
 
+/* ------------------------------------------------------------------ surrogate MLP
+ * The multilayer perceptron behind the learned surrogate (no counterpart in the
+ * reference): BF16 weights and activations, FP32 accumulation, FP32 master weights
+ * and Adam, trained and evaluated by this library's own kernels.  layers linear
+ * maps widths[0] -> widths[1] -> ... -> widths[layers]; GELU after every hidden layer,
+ * none after the last.  Parameters are one float array, layer by layer: W (out x in,
+ * row-major) then b (out).  The loss is the mean squared error over a batch. */
+typedef struct pt_mlp pt_mlp;
+
+pt_status pt_mlp_create(int layers, const int *widths, int max_batch, uint64_t seed, void *cuda_stream,
+                        pt_mlp **out);
+pt_status pt_mlp_param_count(const pt_mlp *mlp, int64_t *count);
+pt_status pt_mlp_set_params(pt_mlp *mlp, const float *params);   /* also clears the Adam state */
+pt_status pt_mlp_get_params(pt_mlp *mlp, float *params);
+/* n rows of inputs (n x widths[0]) and targets (n x widths[layers]) kept on the device */
+pt_status pt_mlp_set_data(pt_mlp *mlp, const float *x, const float *y, int n);
+/* epochs of Adam over the data in shuffled batches; epoch_loss receives the last
+ * epoch's mean loss */
+pt_status pt_mlp_train(pt_mlp *mlp, int epochs, int batch, float lr, uint64_t shuffle_seed, float *epoch_loss);
+/* loss and the gradient of every parameter on n <= max_batch rows (no update) */
+pt_status pt_mlp_gradients(pt_mlp *mlp, const float *x, const float *y, int n, float *grads, float *loss);
+pt_status pt_mlp_predict(pt_mlp *mlp, const float *x, int n, float *y);
+void pt_mlp_destroy(pt_mlp *mlp);
+const char *pt_mlp_last_error(const pt_mlp *mlp);
+
 void pt_destroy(pt_sim *sim);
 
 /* Text of the last error on sim (or of the last failed pt_create when sim is NULL). */

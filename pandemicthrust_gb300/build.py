@@ -23,7 +23,7 @@ LIB = os.path.join(OUT, "libpandemic_gb300.so")
 CLI = os.path.join(OUT, "pt_sim")
 BATCH_CLI = os.path.join(OUT, "pt_batch")
 
-CUDA_SOURCES = ["pt_kernels.cu", "pt_static_table.cu"]
+CUDA_SOURCES = ["pt_kernels.cu", "pt_static_table.cu", "pt_mlp.cu"]
 HOST_SOURCES = ["pt_sim.cpp", "pt_host.cpp"]
 
 

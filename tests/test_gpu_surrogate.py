@@ -1,0 +1,121 @@
+"""The surrogate's network and pipeline: gradients of the hand-written BF16/FP32 kernels
+against an FP64 reference on the CPU, training, and the trained surrogate against the
+method without it (nearest neighbour in the training set), judged by the mean of 32
+simulator replicates."""
+import numpy as np
+import pytest
+from scipy.special import erf
+
+from pandemicthrust_gb300 import surrogate as sg
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16(x):
+    """Round float32 values to bfloat16 (round to nearest even), returned as float64."""
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000).astype(np.uint32)
+    return u.view(np.float32).astype(np.float64)
+
+
+def gelu(z):
+    return 0.5 * z * (1 + erf(z / np.sqrt(2)))
+
+
+def gelu_grad(z):
+    return 0.5 * (1 + erf(z / np.sqrt(2))) + z * np.exp(-0.5 * z * z) / np.sqrt(2 * np.pi)
+
+
+def reference_gradients(params, widths, X, Y):
+    """FP64 forward / backward of the same network; weights and inputs rounded to
+    BF16 as the kernels read them, nothing rounded in between."""
+    Ws, bs, off = [], [], 0
+    for l in range(len(widths) - 1):
+        n = widths[l + 1] * widths[l]
+        Ws.append(bf16(params[off:off + n]).reshape(widths[l + 1], widths[l]))
+        off += n
+        bs.append(params[off:off + widths[l + 1]].astype(np.float64))
+        off += widths[l + 1]
+    H, Hs, Zs = bf16(X), [], []
+    for l, (W, b) in enumerate(zip(Ws, bs)):
+        Hs.append(H)
+        Z = H @ W.T + b
+        Zs.append(Z)
+        H = gelu(Z) if l + 1 < len(Ws) else Z
+    D = H - Y
+    loss = np.mean(D * D)
+    dZ = 2 * D / D.size
+    grads = [None] * (2 * len(Ws))
+    for l in reversed(range(len(Ws))):
+        grads[2 * l] = (dZ.T @ Hs[l]).ravel()
+        grads[2 * l + 1] = dZ.sum(axis=0)
+        if l > 0:
+            dZ = (dZ @ Ws[l]) * gelu_grad(Zs[l - 1])
+    return np.concatenate(grads), loss
+
+
+@pytest.mark.parametrize("widths,batch", [([7, 32, 48, 24], 40), ([7, 256, 256, 218], 128)])
+def test_mlp_gradients_match_fp64_reference(native_lib, widths, batch):
+    rng = np.random.default_rng(7)
+    net = sg.MLP(widths, max_batch=256, seed=3)
+    params = net.get_params()
+    params[:] += rng.normal(0, 0.02, params.size).astype(np.float32)  # non-zero biases too
+    net.set_params(params)
+    X = rng.uniform(0, 1, (batch, widths[0])).astype(np.float32)
+    Y = rng.normal(0, 1, (batch, widths[-1])).astype(np.float32)
+    g, loss = net.gradients(X, Y)
+    ref, ref_loss = reference_gradients(params, widths, X, Y)
+    assert abs(loss - ref_loss) <= 1e-2 * ref_loss
+    off = 0
+    for l in range(len(widths) - 1):
+        for n in (widths[l + 1] * widths[l], widths[l + 1]):
+            a, b = g[off:off + n].astype(np.float64), ref[off:off + n]
+            rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+            assert rel < 3e-2, (l, n, rel)  # BF16 activations and gradients between layers
+            off += n
+    net.close()
+
+
+def test_mlp_learns_a_smooth_map(native_lib):
+    rng = np.random.default_rng(1)
+    X = rng.uniform(0, 1, (2048, 7)).astype(np.float32)
+    Y = np.stack([np.sin(3 * X[:, 0]) * X[:, 1], np.cos(2 * X[:, 2] + X[:, 3]), X[:, 4] * X[:, 5] - X[:, 6]],
+                 axis=1).astype(np.float32)
+    net = sg.MLP([7, 128, 128, 3], max_batch=512, seed=5)
+    net.set_data(X, Y)
+    first = net.train(1, batch=256, lr=1e-3)
+    last = net.train(300, batch=256, lr=1e-3)
+    assert last < first / 20
+    pred = net.predict(X[:100])
+    assert np.sqrt(np.mean((pred - Y[:100]) ** 2)) < 0.1
+    net.close()
+
+
+def test_surrogate_beats_nearest_neighbour_and_falls_back(native_lib):
+    persons = 20_000
+    rng = np.random.default_rng(2024)
+    train = sg.sample_scenarios(384, rng)
+    test = sg.sample_scenarios(12, rng)
+    tr = sg.simulate(train, 1, persons, seed_base=10_000)
+    te = sg.simulate(test, 32, persons, seed_base=50_000)
+    Ytr = sg.targets(tr)[:, 0, :]
+    s = sg.Surrogate(persons, hidden=256, depth=4, seed=1)
+    s.fit(train, Ytr, epochs=800, batch=128, lr=1e-3)
+    pred, fb = s.predict(test)
+    assert not fb.any()
+    truth = sg.summary(te["daily"].mean(axis=1), te["attack"].mean(axis=1))
+    mine = sg.summary(pred["daily"], pred["attack"])
+    nn = sg.decode(sg.nearest_neighbour(sg.features(train), Ytr, sg.features(test)), persons)
+    base = sg.summary(nn["daily"], nn["attack"])
+    pk, at = sg.relative_errors(mine, truth)
+    pk0, at0 = sg.relative_errors(base, truth)
+    assert len(pk) >= 6
+    assert np.median(at) < np.median(at0) and np.median(pk) < np.median(pk0), (np.median(pk), np.median(at),
+                                                                             np.median(pk0), np.median(at0))
+    # an out-of-range scenario is simulated instead
+    odd = dict(test[0], r_pandemic=2.6)
+    p2, fb2 = s.predict([odd, test[1]], fallback_replicates=2, seed_base=77)
+    assert list(fb2) == [True, False]
+    direct = sg.simulate([odd], 2, persons, seed_base=77)
+    assert np.allclose(p2["attack"][0], direct["attack"].mean(axis=1)[0])
+    s.close()
