@@ -320,6 +320,56 @@ def run_batched(args, pt, torch, stream, local):
     }
 
 
+def run_surrogate(args):
+    """The learned surrogate at 1,000,000 persons per scenario: training data from the
+    batched simulator (one run per scenario), a 90/10 split inside fit(), then the
+    error of peak height and attack rate against the mean of 32 simulator replicates
+    of held-out scenarios, and scenarios/s of the surrogate against the batched
+    simulator."""
+    import numpy as np
+    from pandemicthrust_gb300 import surrogate as sg
+    persons, ntest, reps = 1_000_000, 128, 32
+    rng = np.random.default_rng(2025)
+    train = sg.sample_scenarios(args.surrogate_train, rng)
+    test = sg.sample_scenarios(ntest, rng)
+    t0 = time.time()
+    tr = sg.simulate(train, 1, persons, seed_base=10_000)
+    t_train_sim = time.time() - t0
+    t0 = time.time()
+    te = sg.simulate(test, reps, persons, seed_base=50_000_000)
+    t_test_sim = time.time() - t0
+    Y = sg.targets(tr)[:, 0, :]
+    s = sg.Surrogate(persons, seed=1)
+    t0 = time.time()
+    val_loss = s.fit(train, Y, epochs=400, batch=512)
+    t_fit = time.time() - t0
+    pred, _ = s.predict(test)
+    truth = sg.truth_summary(te)
+    pk, at = sg.relative_errors(sg.predicted_summary(pred), truth)
+    nn = sg.decode(sg.nearest_neighbour(sg.features(train), Y, sg.features(test)), persons)
+    pk0, at0 = sg.relative_errors(sg.predicted_summary(nn), truth)
+    X = sg.features(sg.sample_scenarios(262144, np.random.default_rng(5)))
+    s.nets[0].predict(X[:4096])
+    t0 = time.time()
+    s.nets[0].predict(X)
+    t_inf = time.time() - t0
+    s.close()
+    sur_rate = len(X) / t_inf
+    abm_rate = ntest * reps / t_test_sim
+    return {
+        "workload": "surrogate_1M_persons", "train_scenarios": len(train), "test_scenarios": ntest,
+        "test_replicates": reps, "network": "11 -> 4 x 256 GELU -> %d, BF16 weights, FP32 accumulate and Adam" % sg.OUTPUTS,
+        "scenarios_per_s": sur_rate, "abm_scenarios_per_s": abm_rate, "speedup": sur_rate / abm_rate,
+        "error": {"peak_height_median": float(np.median(pk)), "peak_height_mean": float(np.mean(pk)),
+                  "attack_rate_median": float(np.median(at)), "attack_rate_mean": float(np.mean(at)),
+                  "pairs": int(len(pk)), "min_attack": 0.01, "validation_mse": val_loss},
+        "nearest_neighbour_error": {"peak_height_median": float(np.median(pk0)),
+                                    "attack_rate_median": float(np.median(at0))},
+        "target": "<=5% relative error on peak height and attack rate; >=1000x scenarios/s",
+        "seconds": {"train_data": t_train_sim, "test_data": t_test_sim, "fit": t_fit, "inference": t_inf},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -334,6 +384,9 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--batch-warmup", type=int, default=3)
     ap.add_argument("--only-batched", action="store_true", help="run the batched workload alone")
+    ap.add_argument("--surrogate-train", type=int, default=16384,
+                    help="training scenarios of the surrogate section (0: skip it)")
+    ap.add_argument("--only-surrogate", action="store_true", help="run the surrogate section alone")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="population scale (profiling captures only; the bench line is for 1.0)")
     args = ap.parse_args()
@@ -352,6 +405,10 @@ def main():
     if args.only_batched:
         if rank == 0:
             print(json.dumps(run_batched(args, pt, torch, stream, local)))
+        return 0
+    if args.only_surrogate:
+        if rank == 0:
+            print(json.dumps(run_surrogate(args)))
         return 0
     seed = SEED + rank
     params = dict(PARAMS)
@@ -466,6 +523,9 @@ def main():
     batched = None
     if args.batch_instances > 0 and world == 1:
         batched = run_batched(args, pt, torch, stream, local)
+    surrogate = None
+    if args.surrogate_train > 0 and world == 1:
+        surrogate = run_surrogate(args)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -496,6 +556,7 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clocks,
             "batched": batched,
+            "surrogate": surrogate,
         }
         print(json.dumps(line))
     if world > 1:

@@ -22,7 +22,12 @@ from . import PandemicBatch, PtError, load_library, PT_OK
 DAYS = 100
 GENERATIONS = 8          # generational Rn of generations 0..7 per strain
 RN_SCALE = 4.0
-OUTPUTS = 2 * DAYS + 2 + 2 * GENERATIONS
+# outputs: daily infected (2 x DAYS), then per strain attack rate, peak height and
+# peak day, then Rn (2 x GENERATIONS)
+OUTPUTS = 2 * DAYS + 6 + 2 * GENERATIONS
+# the six summary targets (attack rate, peak height, peak day per strain) are scaled
+# up so the squared error weighs them as much as the 200 daily values together
+SUMMARY_WEIGHT = 5.0
 EXPECTED_HOUSEHOLD_SIZE = 2.354
 
 # scenario ranges (inclusive); seeds are sampled and encoded on a log scale
@@ -147,9 +152,15 @@ def in_range(scenarios):
     return np.array([all(RANGES[f][0] <= s[f] <= RANGES[f][1] for f in FEATURES) for s in scenarios])
 
 
+N_DERIVED = 4
+
+
 def features(scenarios):
-    """Inputs of the network: each feature scaled to [0, 1] over its range (seeds on a log scale)."""
-    X = np.zeros((len(scenarios), len(FEATURES)), np.float32)
+    """Inputs of the network: each scenario parameter scaled to [0, 1] over its range
+    (seeds on a log scale), then derived inputs that the dynamics depend on directly:
+    each strain's reproduction number left after vaccination, R (1 - coverage), the
+    day schools reopen, and the closed days within the first 60 days."""
+    X = np.zeros((len(scenarios), len(FEATURES) + N_DERIVED), np.float32)
     for i, s in enumerate(scenarios):
         for j, f in enumerate(FEATURES):
             lo, hi = RANGES[f]
@@ -157,6 +168,12 @@ def features(scenarios):
             if f == "seeds":
                 v, lo, hi = np.log(v), np.log(lo), np.log(hi)
             X[i, j] = (v - lo) / (hi - lo)
+        j = len(FEATURES)
+        X[i, j] = s["r_pandemic"] * (1 - s["vaccination"]) / RANGES["r_pandemic"][1]
+        X[i, j + 1] = s["r_seasonal"] * (1 - s["vaccination"]) / RANGES["r_seasonal"][1]
+        end = s["closure_start"] + s["closure_days"]
+        X[i, j + 2] = end / DAYS
+        X[i, j + 3] = max(0, min(end, 60) - min(s["closure_start"], 60)) / 60.0
     return X
 
 
@@ -215,30 +232,48 @@ def simulate(scenarios, replicates=1, persons=100_000, seed_base=1000, max_perso
 
 
 def targets(sim):
-    """Network targets, one row per (scenario, replicate): log1p(daily) / log1p(N) for
-    each strain, the attack rates, and Rn / RN_SCALE."""
+    """Network targets, one row per (scenario, replicate), each roughly in [0, 1]:
+    log1p(daily infected) / log1p(N) for each strain; per strain log1p(attack * N) /
+    log1p(N), log1p(peak height) / log1p(N) and peak day / DAYS; Rn / RN_SCALE.  Log
+    scales make squared errors behave like relative errors."""
     n, R = sim["attack"].shape[:2]
-    N = sim["persons"].reshape(n, R, 1, 1).astype(np.float64)
-    d = np.log1p(sim["daily"]) / np.log1p(N)
-    Y = np.concatenate([d[..., 0].reshape(n, R, DAYS), d[..., 1].reshape(n, R, DAYS), sim["attack"],
-                        sim["rn"][..., 0] / RN_SCALE, sim["rn"][..., 1] / RN_SCALE], axis=2)
+    N = sim["persons"].reshape(n, R, 1).astype(np.float64)
+    L = np.log1p(N)
+    d = np.log1p(sim["daily"]) / L[..., None]
+    peak = sim["daily"].max(axis=2)                       # n x R x 2
+    peak_day = sim["daily"].argmax(axis=2) / DAYS
+    w = SUMMARY_WEIGHT
+    Y = np.concatenate([d[..., 0], d[..., 1], w * np.log1p(sim["attack"] * N) / L, w * np.log1p(peak) / L,
+                        w * peak_day, sim["rn"][..., 0] / RN_SCALE, sim["rn"][..., 1] / RN_SCALE], axis=2)
     return Y.astype(np.float32)
 
 
 def decode(Y, persons):
-    """Network outputs -> daily infected (n x DAYS x 2), attack rates (n x 2), Rn."""
+    """Network outputs -> daily infected (n x DAYS x 2) and, per strain, attack rate,
+    peak height and peak day (n x 2), and Rn (n x GENERATIONS x 2)."""
     Y = np.asarray(Y, np.float64)
     L = np.log1p(persons)
+    o = 2 * DAYS
     daily = np.stack([np.expm1(np.clip(Y[:, :DAYS], 0, None) * L),
-                      np.expm1(np.clip(Y[:, DAYS:2 * DAYS], 0, None) * L)], axis=2)
-    attack = np.clip(Y[:, 2 * DAYS:2 * DAYS + 2], 0.0, 1.0)
-    rn = np.stack([Y[:, 2 * DAYS + 2:2 * DAYS + 2 + GENERATIONS], Y[:, 2 * DAYS + 2 + GENERATIONS:]], axis=2)
-    return {"daily": daily, "attack": attack, "rn": rn * RN_SCALE}
+                      np.expm1(np.clip(Y[:, DAYS:o], 0, None) * L)], axis=2)
+    S = Y[:, o:o + 6] / SUMMARY_WEIGHT
+    attack = np.clip(np.expm1(np.clip(S[:, 0:2], 0, None) * L) / persons, 0.0, 1.0)
+    peak = np.expm1(np.clip(S[:, 2:4], 0, None) * L)
+    peak_day = np.clip(np.rint(S[:, 4:6] * DAYS), 0, DAYS - 1)
+    rn = np.stack([Y[:, o + 6:o + 6 + GENERATIONS], Y[:, o + 6 + GENERATIONS:]], axis=2)
+    return {"daily": daily, "attack": attack, "peak": peak, "peak_day": peak_day, "rn": rn * RN_SCALE}
 
 
-def summary(daily, attack):
-    """Peak height (infected on the peak day), peak day and attack rate per strain."""
-    return {"peak": daily.max(axis=1), "peak_day": daily.argmax(axis=1), "attack": np.asarray(attack)}
+def truth_summary(sim):
+    """The judge of the surrogate: per scenario and strain, the mean over replicates of
+    peak height (infected on the peak day), peak day and attack rate."""
+    return {"peak": sim["daily"].max(axis=2).mean(axis=1), "peak_day": sim["daily"].argmax(axis=2).mean(axis=1),
+            "attack": sim["attack"].mean(axis=1)}
+
+
+def predicted_summary(pred):
+    """The same quantities as the surrogate predicts them."""
+    return {"peak": pred["peak"], "peak_day": pred["peak_day"], "attack": pred["attack"]}
 
 
 def relative_errors(pred, truth, min_attack=0.01):
@@ -252,33 +287,73 @@ def relative_errors(pred, truth, min_attack=0.01):
 
 
 class Surrogate:
-    """MLP surrogate for one population size, with the simulator as fallback."""
+    """MLP surrogate for one population size (an ensemble of `members` networks
+    averaged in target space), with the simulator as fallback."""
 
-    def __init__(self, persons=100_000, hidden=256, depth=4, seed=0, max_batch=4096):
+    # fractions of the epochs and their learning rates: a stepped decay
+    SCHEDULE = ((0.5, 1e-3), (0.3, 3e-4), (0.2, 1e-4))
+
+    def __init__(self, persons=100_000, hidden=256, depth=4, seed=0, max_batch=4096, members=1):
         self.persons = int(persons)
-        self.net = MLP([len(FEATURES)] + [hidden] * depth + [OUTPUTS], max_batch=max_batch, seed=seed)
+        self.nets = [MLP([len(FEATURES) + N_DERIVED] + [hidden] * depth + [OUTPUTS], max_batch=max_batch,
+                         seed=seed + 7919 * i)
+                     for i in range(members)]
 
-    def fit(self, scenarios, Y, epochs=1500, batch=256, lr=1e-3, seed=0):
-        """Trains on one target row per scenario (average replicates before, or pass
-        each replicate as its own row)."""
-        self.net.set_data(features(scenarios), Y)
-        return self.net.train(epochs, batch=batch, lr=lr, seed=seed)
+    def fit(self, scenarios, Y, epochs=400, batch=512, val_fraction=0.1, checks=16, seed=0):
+        """Trains every member on one target row per scenario (average replicates
+        before, or pass each replicate as its own row), holding out val_fraction of
+        the rows: the learning rate follows SCHEDULE over `epochs`, the validation
+        loss is measured `checks` times, and each member keeps its best weights.
+        Returns the mean best validation loss."""
+        X = np.asarray(features(scenarios), np.float32)
+        Y = np.asarray(Y, np.float32)
+        order = np.random.default_rng(seed).permutation(len(X))
+        nv = int(len(X) * val_fraction)
+        val, trn = order[:nv], order[nv:]
+        best_losses = []
+        for i, net in enumerate(self.nets):
+            net.set_data(X[trn], Y[trn])
+            best, best_params = np.inf, net.get_params()
+            done = 0
+            step = max(1, epochs // checks)
+            for j, (frac, rate) in enumerate(self.SCHEDULE):
+                phase_end = done + max(1, int(round(epochs * frac)))
+                while done < phase_end:
+                    n = min(step, phase_end - done)
+                    net.train(n, batch=batch, lr=rate, seed=seed + 101 * i + 7 * done)
+                    done += n
+                    if nv:
+                        v = float(np.mean((net.predict(X[val]) - Y[val]) ** 2))
+                        if v < best:
+                            best, best_params = v, net.get_params()
+            if nv:
+                net.set_params(best_params)
+            best_losses.append(best)
+        return float(np.mean(best_losses))
+
+    def raw(self, scenarios):
+        X = features(scenarios)
+        return np.mean([net.predict(X) for net in self.nets], axis=0)
 
     def predict(self, scenarios, fallback_replicates=4, seed_base=900_000):
         """Decoded predictions; scenarios outside the training ranges are simulated
         instead (mean of fallback_replicates runs).  Also returns the fallback mask."""
         ok = in_range(scenarios)
-        out = decode(self.net.predict(features(scenarios)), self.persons)
+        out = decode(self.raw(scenarios), self.persons)
         if not ok.all():
             idx = np.nonzero(~ok)[0]
             sim = simulate([scenarios[i] for i in idx], fallback_replicates, self.persons, seed_base)
+            t = truth_summary(sim)
             out["daily"][idx] = sim["daily"].mean(axis=1)
-            out["attack"][idx] = sim["attack"].mean(axis=1)
+            out["attack"][idx] = t["attack"]
+            out["peak"][idx] = t["peak"]
+            out["peak_day"][idx] = t["peak_day"]
             out["rn"][idx] = sim["rn"].mean(axis=1)
         return out, ~ok
 
     def close(self):
-        self.net.close()
+        for net in self.nets:
+            net.close()
 
 
 def nearest_neighbour(train_X, train_Y, X):

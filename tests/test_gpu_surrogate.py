@@ -54,7 +54,7 @@ def reference_gradients(params, widths, X, Y):
     return np.concatenate(grads), loss
 
 
-@pytest.mark.parametrize("widths,batch", [([7, 32, 48, 24], 40), ([7, 256, 256, 218], 128)])
+@pytest.mark.parametrize("widths,batch", [([7, 32, 48, 24], 40), ([7, 256, 256, 222], 128)])
 def test_mlp_gradients_match_fp64_reference(native_lib, widths, batch):
     rng = np.random.default_rng(7)
     net = sg.MLP(widths, max_batch=256, seed=3)
@@ -100,13 +100,13 @@ def test_surrogate_beats_nearest_neighbour_and_falls_back(native_lib):
     te = sg.simulate(test, 32, persons, seed_base=50_000)
     Ytr = sg.targets(tr)[:, 0, :]
     s = sg.Surrogate(persons, hidden=256, depth=4, seed=1)
-    s.fit(train, Ytr, epochs=800, batch=128, lr=1e-3)
+    s.fit(train, Ytr, epochs=600, batch=128, checks=6)
     pred, fb = s.predict(test)
     assert not fb.any()
-    truth = sg.summary(te["daily"].mean(axis=1), te["attack"].mean(axis=1))
-    mine = sg.summary(pred["daily"], pred["attack"])
+    truth = sg.truth_summary(te)
+    mine = sg.predicted_summary(pred)
     nn = sg.decode(sg.nearest_neighbour(sg.features(train), Ytr, sg.features(test)), persons)
-    base = sg.summary(nn["daily"], nn["attack"])
+    base = sg.predicted_summary(nn)
     pk, at = sg.relative_errors(mine, truth)
     pk0, at0 = sg.relative_errors(base, truth)
     assert len(pk) >= 6
