@@ -98,13 +98,16 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g)
             for (int q = 0; q < 4; q++) acc[a][b][q] = 0.f;
     const bf16 zero = __float2bfloat16(0.f);
     for (int r0 = 0; r0 < g.R; r0 += kTileK) {
+        // consecutive threads read consecutive addresses: the index with stride 1 varies fastest
         for (int e = threadIdx.x; e < kTile * kTileK; e += 128) {
-            const int i = e / kTileK, r = e % kTileK;
+            const bool r_fast = g.sa_r == 1;
+            const int i = r_fast ? e / kTileK : e % kTile, r = r_fast ? e % kTileK : e / kTile;
             const int gi = bm + i, gr = r0 + r;
             As[i][r] = (gi < g.M && gr < g.R) ? g.A[gi * g.sa_i + gr * g.sa_r] : zero;
         }
         for (int e = threadIdx.x; e < kTileK * kTile; e += 128) {
-            const int r = e / kTile, j = e % kTile;
+            const bool j_fast = g.sb_j == 1;
+            const int r = j_fast ? e / kTile : e % kTileK, j = j_fast ? e % kTile : e / kTileK;
             const int gr = r0 + r, gj = bn + j;
             Bs[r][j] = (gr < g.R && gj < g.N) ? g.B[gr * g.sb_r + gj * g.sb_j] : zero;
         }
