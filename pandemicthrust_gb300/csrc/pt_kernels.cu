@@ -92,6 +92,7 @@ cudaError_t launch_household_types(const SimConst &c, uint8_t *types, int32_t *s
 // for each radix pass p, the histogram of the key's 8-bit digit p weighted by the
 // count (digit_hist[p][256]), from which the radix sort takes its digit bases.
 constexpr int kScanThreads = 256, kScanItems = 16, kScanTile = kScanThreads * kScanItems;
+static_assert(kScanTile == kScanTileEntries, "the host sizes the scan look-back words by kScanTileEntries");
 constexpr int kMaxRadixPasses = 4;
 
 __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *in, int32_t *out, int n, int clear_in,
@@ -321,6 +322,7 @@ cudaError_t launch_count_keys(const int32_t *keys, int n, int32_t *count, cudaSt
 constexpr int kRadixThreads = 256, kRadixWarps = 8, kRadixItems = 16;
 constexpr int kRadixWarpItems = kRadixItems * 32;
 constexpr int kRadixTile = kRadixThreads * kRadixItems;
+static_assert(kRadixTile == kRadixTileEntries, "the host sizes the radix look-back words by kRadixTileEntries");
 
 enum RadixMode { kRadixFirst = 0, kRadixMiddle = 1, kRadixLast = 2, kRadixOnly = 3 };
 

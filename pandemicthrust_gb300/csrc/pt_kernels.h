@@ -11,6 +11,8 @@ constexpr int kTypes = 14;
 constexpr int kMaxDays = 256;
 
 constexpr int kPersonTile = 4096;  // persons per sweep / schedule tile
+constexpr int kRadixTileEntries = 4096;  // entries per radix-pass tile (256 look-back words each)
+constexpr int kScanTileEntries = 4096;   // values per scan tile (one look-back word each)
 constexpr int kDigitStripes = 16;  // copies of the day's radix digit histograms (spreads the updates)
 
 // Constants of one simulation (setup kernels take them by value; the day kernels

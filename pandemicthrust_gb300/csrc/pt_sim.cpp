@@ -268,7 +268,7 @@ static pt_status engine_setup(Engine *s)
             return fail(s, PT_ERR_ARG, "batch too large for 32-bit ids");
     }
     const long long Bday = std::max(B0, B1), Bmax = std::max(Bday, LT + 1);
-    const long long tiles_cap = std::max({maxP, Bmax + 1, HS + 1}) / 4096 + 4;
+    const long long tiles_cap = std::max({maxP, Bmax + 1, HS + 1}) / ptk::kScanTileEntries + 4;
 
     // small block: scalars, look-back tiles and control words, instance records and
     // state, generation histograms, household offsets, setup counters
@@ -359,7 +359,8 @@ static pt_status engine_setup(Engine *s)
 
     // arena of per-person and per-location arrays
     const size_t n = (size_t)P, ntiles = n / ptk::kPersonTile;
-    const size_t radix_tiles = (3 * n + 4095) / 4096 + 1 + (size_t)K;  // segments round up to whole tiles
+    const size_t radix_tiles =  // segments round up to whole tiles
+        (3 * n + ptk::kRadixTileEntries - 1) / ptk::kRadixTileEntries + 1 + (size_t)K;
     int nseeds = 0;
     for (const Instance &in : s->inst) nseeds += in.params.initial_pandemic + in.params.initial_seasonal;
     size_t bytes = 0;
