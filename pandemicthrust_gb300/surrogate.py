@@ -14,6 +14,9 @@ extensions, built on the batched engine (``PandemicBatch``) and the intervention
 hooks (``pt_set_interventions``).
 """
 import ctypes
+import json
+import os
+import time
 
 import numpy as np
 
@@ -41,6 +44,9 @@ RANGES = {
     "vaccination": (0.0, 0.5),
 }
 FEATURES = tuple(RANGES)
+# the surrogate shipped with the package (1,000,000 persons per scenario; made by
+# `python -m pandemicthrust_gb300.surrogate build --out <this path>`)
+SHIPPED_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "models", "surrogate_1m.npz")
 
 
 class MLP:
@@ -351,9 +357,63 @@ class Surrogate:
             out["rn"][idx] = sim["rn"].mean(axis=1)
         return out, ~ok
 
+    # ------------------------------------------------------------ saved models
+    def _meta(self):
+        return dict(persons=self.persons, widths=self.nets[0].widths, members=len(self.nets),
+                    features=list(FEATURES), ranges={k: list(v) for k, v in RANGES.items()}, days=DAYS,
+                    generations=GENERATIONS, rn_scale=RN_SCALE, summary_weight=SUMMARY_WEIGHT,
+                    n_derived=N_DERIVED, outputs=OUTPUTS)
+
+    def save(self, path, **info):
+        """Writes every member's parameters as inference uses them: weight matrices as
+        BF16, biases in FP32 (the GEMM epilogue adds the FP32 bias), with the model's
+        shape and target encoding (and any `info`, e.g. how it was trained)."""
+        mask = _bias_mask(self.nets[0].widths)
+        p = [net.get_params() for net in self.nets]
+        meta = dict(self._meta(), info=info)
+        np.savez_compressed(path, params=np.stack([_bf16_bits(q) for q in p]),
+                            biases=np.stack([q[mask] for q in p]), meta=np.array(json.dumps(meta)))
+
+    @classmethod
+    def load(cls, path, max_batch=4096):
+        """A surrogate saved by save(); refuses a file whose features, ranges or
+        target encoding differ from this module's."""
+        z = np.load(path)
+        meta = json.loads(str(z["meta"]))
+        w = meta["widths"]
+        s = cls(meta["persons"], hidden=w[1], depth=len(w) - 2, max_batch=max_batch, members=meta["members"])
+        want = s._meta()
+        for k, v in want.items():
+            if k != "members" and meta.get(k) != v:
+                s.close()
+                raise ValueError("%s: %s is %r, this module has %r" % (path, k, meta.get(k), v))
+        mask = _bias_mask(w)
+        for net, bits, bias in zip(s.nets, z["params"], z["biases"]):
+            v = _bf16_values(bits)
+            v[mask] = bias
+            net.set_params(v)
+        s.info = meta.get("info", {})
+        return s
+
     def close(self):
         for net in self.nets:
             net.close()
+
+
+def _bias_mask(widths):
+    """Bias positions in the parameter array: each layer stores W (out x in), then b."""
+    return np.concatenate([np.r_[np.zeros(widths[i] * widths[i + 1], bool), np.ones(widths[i + 1], bool)]
+                           for i in range(len(widths) - 1)])
+
+
+def _bf16_bits(a):
+    """float32 -> BF16 bit patterns, rounded to nearest even (as the device rounds)."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+def _bf16_values(bits):
+    return (np.asarray(bits, np.uint16).astype(np.uint32) << 16).view(np.float32)
 
 
 def nearest_neighbour(train_X, train_Y, X):
@@ -361,3 +421,72 @@ def nearest_neighbour(train_X, train_Y, X):
     training scenario in feature space."""
     d = ((X[:, None, :] - train_X[None, :, :]) ** 2).sum(axis=2)
     return train_Y[d.argmin(axis=1)]
+
+
+def evaluate(surrogate, scenarios, replicates, seed_base):
+    """Errors of a surrogate against the mean of `replicates` simulator runs of each
+    scenario, and the time both took."""
+    t0 = time.time()
+    sim = simulate(scenarios, replicates, surrogate.persons, seed_base=seed_base)
+    t_sim = time.time() - t0
+    t0 = time.time()
+    pred = decode(surrogate.raw(scenarios), surrogate.persons)
+    t_pred = time.time() - t0
+    pk, at = relative_errors(predicted_summary(pred), truth_summary(sim))
+    return {"pairs": int(len(pk)), "peak_median": float(np.median(pk)), "peak_mean": float(np.mean(pk)),
+            "attack_median": float(np.median(at)), "attack_mean": float(np.mean(at)),
+            "simulate_s": t_sim, "predict_s": t_pred}
+
+
+def main(argv=None):
+    """python -m pandemicthrust_gb300.surrogate build|evaluate ...
+
+    build: samples scenarios, simulates each once on the batched simulator, trains
+    an ensemble and saves it.  evaluate: scores a saved surrogate against fresh
+    simulations (mean of replicates)."""
+    import argparse
+    ap = argparse.ArgumentParser(prog="python -m pandemicthrust_gb300.surrogate")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    b = sub.add_parser("build")
+    b.add_argument("--out", required=True)
+    b.add_argument("--persons", type=int, default=1_000_000)
+    b.add_argument("--train", type=int, default=131072)
+    b.add_argument("--members", type=int, default=4)
+    b.add_argument("--epochs", type=int, default=200)
+    b.add_argument("--batch", type=int, default=512)
+    b.add_argument("--hidden", type=int, default=256)
+    b.add_argument("--depth", type=int, default=4)
+    b.add_argument("--seed", type=int, default=7, help="scenario sampling and network initialisation")
+    b.add_argument("--seed-base", type=int, default=1_000_000, help="core seed of the first simulation")
+    e = sub.add_parser("evaluate")
+    e.add_argument("--model", required=True)
+    e.add_argument("--test", type=int, default=1024)
+    e.add_argument("--replicates", type=int, default=16)
+    e.add_argument("--seed", type=int, default=99)
+    e.add_argument("--seed-base", type=int, default=70_000_000)
+    a = ap.parse_args(argv)
+    if a.cmd == "build":
+        scen = sample_scenarios(a.train, np.random.default_rng(a.seed))
+        t0 = time.time()
+        sim = simulate(scen, 1, a.persons, seed_base=a.seed_base)
+        t_sim = time.time() - t0
+        s = Surrogate(a.persons, hidden=a.hidden, depth=a.depth, seed=a.seed, members=a.members)
+        t0 = time.time()
+        val = s.fit(scen, targets(sim)[:, 0, :], epochs=a.epochs, batch=a.batch)
+        t_fit = time.time() - t0
+        info = {"train_scenarios": a.train, "persons": a.persons, "epochs": a.epochs, "batch": a.batch,
+                "scenario_seed": a.seed, "seed_base": a.seed_base, "val_loss": val, "simulate_s": t_sim,
+                "fit_s": t_fit}
+        s.save(a.out, **info)
+        s.close()
+        print(json.dumps(info))
+    else:
+        s = Surrogate.load(a.model)
+        scen = sample_scenarios(a.test, np.random.default_rng(a.seed))
+        r = evaluate(s, scen, a.replicates, a.seed_base)
+        s.close()
+        print(json.dumps(dict(r, test_scenarios=a.test, replicates=a.replicates)))
+
+
+if __name__ == "__main__":
+    main()

@@ -119,3 +119,20 @@ def test_surrogate_beats_nearest_neighbour_and_falls_back(native_lib):
     direct = sg.simulate([odd], 2, persons, seed_base=77)
     assert np.allclose(p2["attack"][0], direct["attack"].mean(axis=1)[0])
     s.close()
+
+
+def test_saved_surrogate_predicts_the_same(native_lib, tmp_path):
+    rng = np.random.default_rng(3)
+    scen = sg.sample_scenarios(64, rng)
+    s = sg.Surrogate(20_000, hidden=32, depth=2, seed=5, members=2)
+    Y = rng.random((64, sg.OUTPUTS)).astype(np.float32)
+    s.fit(scen, Y, epochs=4, batch=16, checks=2)
+    path = tmp_path / "model.npz"
+    s.save(path, note="test")
+    before = s.raw(scen)
+    s.close()
+    t = sg.Surrogate.load(path)
+    assert t.persons == 20_000 and len(t.nets) == 2 and t.info == {"note": "test"}
+    # the saved weights are the BF16 values inference uses: predictions are identical
+    np.testing.assert_array_equal(t.raw(scen), before)
+    t.close()

@@ -1,0 +1,53 @@
+"""Host-side pieces of the surrogate: BF16 weight files and the target encoding."""
+import json
+
+import numpy as np
+import pytest
+
+from pandemicthrust_gb300 import surrogate as sg
+
+
+def test_bf16_bits_round_to_nearest_even():
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(0)
+    a = np.concatenate([rng.standard_normal(10000).astype(np.float32) * 10.0 ** rng.integers(-6, 6, 10000),
+                        np.array([1.0, 1.00390625, 1.01171875, -1.00390625, 0.0, -0.0], np.float32)])
+    want = torch.tensor(a).bfloat16().float().numpy()
+    got = sg._bf16_values(sg._bf16_bits(a))
+    np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_targets_decode_round_trip():
+    rng = np.random.default_rng(1)
+    n, N = 5, 1_000_000
+    daily = np.zeros((n, 1, sg.DAYS, 2))
+    for i in range(n):
+        t = np.arange(sg.DAYS)
+        for s in range(2):
+            daily[i, 0, :, s] = np.rint(rng.uniform(1e3, 1e5) * np.exp(-((t - rng.uniform(20, 90)) / 15.0) ** 2))
+    sim = {"daily": daily, "attack": rng.uniform(0.01, 0.9, (n, 1, 2)), "rn": rng.uniform(0, 3, (n, 1, 8, 2)),
+           "persons": np.full((n, 1), N)}
+    d = sg.decode(sg.targets(sim)[:, 0, :], N)
+    np.testing.assert_allclose(d["attack"], sim["attack"][:, 0], rtol=1e-5)
+    np.testing.assert_allclose(d["peak"], daily[:, 0].max(axis=1), rtol=1e-5)
+    np.testing.assert_array_equal(d["peak_day"], daily[:, 0].argmax(axis=1))
+    np.testing.assert_allclose(d["rn"], sim["rn"][:, 0], rtol=1e-5)
+
+
+def test_shipped_model_matches_this_module():
+    """The committed surrogate was trained for these features, ranges and outputs."""
+    import os
+    path = sg.SHIPPED_MODEL
+    if not os.path.exists(path):
+        pytest.skip("no shipped surrogate")
+    z = np.load(path)
+    meta = json.loads(str(z["meta"]))
+    assert meta["features"] == list(sg.FEATURES)
+    assert meta["ranges"] == {k: list(v) for k, v in sg.RANGES.items()}
+    assert meta["outputs"] == sg.OUTPUTS and meta["summary_weight"] == sg.SUMMARY_WEIGHT
+    w = meta["widths"]
+    n = sum(w[i] * w[i + 1] + w[i + 1] for i in range(len(w) - 1))
+    assert z["params"].shape == (meta["members"], n) and z["params"].dtype == np.uint16
+    nb = sum(w[1:])
+    assert z["biases"].shape == (meta["members"], nb) and z["biases"].dtype == np.float32
+    assert sg._bias_mask(w).sum() == nb
