@@ -358,9 +358,9 @@ def run_surrogate(args):
     if os.path.exists(sg.SHIPPED_MODEL):
         s = sg.Surrogate.load(sg.SHIPPED_MODEL)
         pred, _ = s.predict(test)
-        s.raw(X[:4096])
+        s.raw_features(X[:4096])
         t0 = time.time()
-        s.raw(X)   # every member of the ensemble
+        s.raw_features(X)   # every member of the ensemble
         t_inf = time.time() - t0
         out["model"] = dict(s.info, file=os.path.relpath(sg.SHIPPED_MODEL, ROOT), members=len(s.nets))
         out["error"] = errors(pred)

@@ -338,7 +338,11 @@ class Surrogate:
         return float(np.mean(best_losses))
 
     def raw(self, scenarios):
-        X = features(scenarios)
+        """Ensemble mean of the network outputs (target space) for scenario dicts."""
+        return self.raw_features(features(scenarios))
+
+    def raw_features(self, X):
+        """The same for rows of features() already computed."""
         return np.mean([net.predict(X) for net in self.nets], axis=0)
 
     def predict(self, scenarios, fallback_replicates=4, seed_base=900_000):
