@@ -84,18 +84,36 @@ def measured_peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per launch of the profiled kernel, from the committed ncu summary."""
+def ncu_records(kind):
+    """`kind` lines of the committed ncu summary (profiles/ncu_traffic.txt), by stage."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     out = {}
     try:
         for line in open(path):
-            if line.startswith("traffic "):
+            if line.startswith(kind + " "):
                 kv = dict(x.split("=", 1) for x in line.split()[1:])
-                out[kv["stage"]] = float(kv["bytes_per_launch"])
+                out[kv.pop("stage")] = kv
     except Exception:
         pass
     return out
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the profiled kernel, from the committed ncu summary."""
+    return {k: float(v["bytes_per_launch"]) for k, v in ncu_records("traffic").items()}
+
+
+def int_roof(stage, n_weekday, n_weekend):
+    """The integer-pipe roof of a Threefry-bound kernel: ALU-pipe utilisation
+    (IADD3/LOP3/SHF) from the committed ncu capture, weighted by this run's weekday
+    and weekend launches."""
+    r = ncu_records("pipe").get(stage)
+    if not r:
+        return None
+    wd, we = float(r["alu_weekday"]), float(r["alu_weekend"])
+    n = max(n_weekday + n_weekend, 1)
+    return {"kernel": stage, "pipe": "alu (int32)", "frac": (wd * n_weekday + we * n_weekend) / n,
+            "weekday": wd, "weekend": we, "source": "profiles/" + r["source"]}
 
 
 class ClockSampler:
@@ -577,6 +595,7 @@ def main():
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic},
+            "int_roofline": int_roof(dominant, nwd, nwe),
             "day_roofline": {"achieved": day_achieved, "peak": peak, "unit": "GB/s", "frac": day_achieved / peak,
                              "bytes_per_run": all_bytes},
             "stages": breakdown,
