@@ -51,3 +51,45 @@ def test_shipped_model_matches_this_module():
     nb = sum(w[1:])
     assert z["biases"].shape == (meta["members"], nb) and z["biases"].dtype == np.float32
     assert sg._bias_mask(w).sum() == nb
+
+
+class _FakeNet:
+    """Stands in for MLP: its 'weights' count the epochs trained so far."""
+
+    def __init__(self):
+        self.calls, self.p, self.widths = [], np.zeros(3, np.float32), [11, 4, sg.OUTPUTS]
+
+    def set_data(self, X, Y):
+        pass
+
+    def get_params(self):
+        return self.p.copy()
+
+    def set_params(self, p):
+        self.p = np.array(p, np.float32)
+
+    def train(self, n, batch, lr, seed):
+        self.calls.append((n, lr))
+        self.p = self.p + n
+
+    def predict(self, X):
+        return np.zeros((len(X), sg.OUTPUTS), np.float32)
+
+
+@pytest.mark.parametrize("epochs,average_last", [(400, None), (200, 40), (50, 0), (7, None)])
+def test_fit_follows_the_schedule_and_averages_the_last_epochs(epochs, average_last):
+    s = sg.Surrogate.__new__(sg.Surrogate)
+    s.persons, s.nets = 1, [_FakeNet(), _FakeNet()]
+    scen = sg.sample_scenarios(40, np.random.default_rng(0))
+    s.fit(scen, np.zeros((40, sg.OUTPUTS), np.float32), epochs=epochs, checks=16, average_last=average_last)
+    rates = [r for f, r in sg.Surrogate.SCHEDULE for _ in range(max(1, int(round(epochs * f))))]
+    for net in s.nets:
+        # every epoch trained once, at its scheduled rate
+        assert [lr for n, lr in net.calls for _ in range(n)] == rates
+        avg = int(round(epochs * sg.Surrogate.SCHEDULE[-1][0])) if average_last is None else average_last
+        if avg:
+            # the weights are the mean over the last `avg` epochs
+            want = np.mean(np.arange(len(rates) - avg + 1, len(rates) + 1))
+            np.testing.assert_allclose(net.p, want, rtol=1e-6)
+        else:
+            assert net.p[0] == net.calls[0][0]   # equal validation losses keep the first checkpoint
