@@ -351,7 +351,7 @@ def run_surrogate(args):
     the trainer, with nearest neighbour in its training set as the baseline."""
     import numpy as np
     from pandemicthrust_gb300 import surrogate as sg
-    persons, ntest, reps = 1_000_000, 512, 16
+    persons, ntest, reps = 1_000_000, 256, 32
     rng = np.random.default_rng(2025)
     train = sg.sample_scenarios(args.surrogate_train, rng)
     test = sg.sample_scenarios(ntest, rng)
@@ -363,8 +363,10 @@ def run_surrogate(args):
 
     def errors(pred):
         pk, at = sg.relative_errors(sg.predicted_summary(pred), truth)
+        pd = sg.peak_day_errors(pred, truth)
         return {"peak_height_median": float(np.median(pk)), "peak_height_mean": float(np.mean(pk)),
                 "attack_rate_median": float(np.median(at)), "attack_rate_mean": float(np.mean(at)),
+                "peak_day_abs_days_median": float(np.median(pd)), "peak_day_abs_days_mean": float(np.mean(pd)),
                 "pairs": int(len(pk)), "min_attack": 0.01}
 
     X = sg.features(sg.sample_scenarios(262144, np.random.default_rng(5)))

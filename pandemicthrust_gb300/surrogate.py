@@ -282,6 +282,13 @@ def predicted_summary(pred):
     return {"peak": pred["peak"], "peak_day": pred["peak_day"], "attack": pred["attack"]}
 
 
+def peak_day_errors(pred, truth, min_attack=0.01):
+    """|predicted - reference| peak day in days, over the same pairs as
+    relative_errors (the reference is the mean peak day of the replicates)."""
+    mask = truth["attack"] >= min_attack
+    return np.abs(np.asarray(pred["peak_day"], np.float64) - truth["peak_day"])[mask]
+
+
 def relative_errors(pred, truth, min_attack=0.01):
     """|pred - truth| / truth of peak height and attack rate, for (scenario, strain)
     pairs whose reference attack rate is at least min_attack (an epidemic that dies
@@ -456,9 +463,12 @@ def evaluate(surrogate, scenarios, replicates, seed_base):
     t0 = time.time()
     pred = decode(surrogate.raw(scenarios), surrogate.persons)
     t_pred = time.time() - t0
-    pk, at = relative_errors(predicted_summary(pred), truth_summary(sim))
+    truth = truth_summary(sim)
+    pk, at = relative_errors(predicted_summary(pred), truth)
+    pd = peak_day_errors(pred, truth)
     return {"pairs": int(len(pk)), "peak_median": float(np.median(pk)), "peak_mean": float(np.mean(pk)),
             "attack_median": float(np.median(at)), "attack_mean": float(np.mean(at)),
+            "peak_day_abs_median": float(np.median(pd)), "peak_day_abs_mean": float(np.mean(pd)),
             "simulate_s": t_sim, "predict_s": t_pred}
 
 
@@ -487,7 +497,7 @@ def main(argv=None):
     e = sub.add_parser("evaluate")
     e.add_argument("--model", required=True)
     e.add_argument("--test", type=int, default=1024)
-    e.add_argument("--replicates", type=int, default=16)
+    e.add_argument("--replicates", type=int, default=32)
     e.add_argument("--seed", type=int, default=99)
     e.add_argument("--seed-base", type=int, default=70_000_000)
     a = ap.parse_args(argv)
