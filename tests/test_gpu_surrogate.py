@@ -136,3 +136,20 @@ def test_saved_surrogate_predicts_the_same(native_lib, tmp_path):
     # the saved weights are the BF16 values inference uses: predictions are identical
     np.testing.assert_array_equal(t.raw(scen), before)
     t.close()
+
+
+def test_shipped_surrogate_on_fresh_scenarios(native_lib):
+    """The shipped ensemble against simulations it never saw (new draws, new seeds).
+    A small sample with a loose bound; the full evaluation (1,024 scenarios x 32
+    replicates) gives 3.9% / 3.4% median peak / attack error."""
+    import os
+    if not os.path.exists(sg.SHIPPED_MODEL):
+        pytest.skip("no shipped surrogate")
+    s = sg.Surrogate.load(sg.SHIPPED_MODEL)
+    assert s.persons == 1_000_000 and len(s.nets) >= 1
+    scen = sg.sample_scenarios(48, np.random.default_rng(4242))
+    r = sg.evaluate(s, scen, 8, seed_base=90_000_000)
+    s.close()
+    assert r["pairs"] >= 10
+    assert r["peak_median"] < 0.08 and r["attack_median"] < 0.08, r
+    assert r["peak_day_abs_median"] <= 3, r
