@@ -208,7 +208,9 @@ def run_reference(args, world, rank):
     from oracle import build_oracle
     from oracle.oracle import Oracle
     build_oracle.build()
-    o = Oracle(PARAMS, SEED, threads=threads)
+    params = dict(PARAMS)
+    params["people_scaling"] = PARAMS["people_scaling"] * args.scale
+    o = Oracle(params, SEED, threads=threads)
     o.setup()
     N = o.view()["N"]
     for _ in range(args.warmup):
