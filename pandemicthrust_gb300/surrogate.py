@@ -390,10 +390,7 @@ class Surrogate:
 
     # ------------------------------------------------------------ saved models
     def _meta(self):
-        return dict(persons=self.persons, widths=self.nets[0].widths, members=len(self.nets),
-                    features=list(FEATURES), ranges={k: list(v) for k, v in RANGES.items()}, days=DAYS,
-                    generations=GENERATIONS, rn_scale=RN_SCALE, summary_weight=SUMMARY_WEIGHT,
-                    n_derived=N_DERIVED, outputs=OUTPUTS)
+        return dict(_encoding(), persons=self.persons, widths=self.nets[0].widths, members=len(self.nets))
 
     def save(self, path, **info):
         """Writes every member's parameters as inference uses them: weight matrices as
@@ -411,13 +408,13 @@ class Surrogate:
         target encoding differ from this module's."""
         z = np.load(path)
         meta = json.loads(str(z["meta"]))
-        w = meta["widths"]
-        s = cls(meta["persons"], hidden=w[1], depth=len(w) - 2, max_batch=max_batch, members=meta["members"])
-        want = s._meta()
-        for k, v in want.items():
-            if k != "members" and meta.get(k) != v:
-                s.close()
+        for k, v in _encoding().items():
+            if meta.get(k) != v:
                 raise ValueError("%s: %s is %r, this module has %r" % (path, k, meta.get(k), v))
+        w = meta["widths"]
+        if w[0] != len(FEATURES) + N_DERIVED or w[-1] != OUTPUTS or len(set(w[1:-1])) != 1:
+            raise ValueError("%s: layer widths %r do not fit this module's network" % (path, w))
+        s = cls(meta["persons"], hidden=w[1], depth=len(w) - 2, max_batch=max_batch, members=meta["members"])
         mask = _bias_mask(w)
         for net, bits, bias in zip(s.nets, z["params"], z["biases"]):
             v = _bf16_values(bits)
@@ -429,6 +426,13 @@ class Surrogate:
     def close(self):
         for net in self.nets:
             net.close()
+
+
+def _encoding():
+    """What a saved surrogate must share with this module: its inputs and targets."""
+    return dict(features=list(FEATURES), ranges={k: list(v) for k, v in RANGES.items()}, days=DAYS,
+                generations=GENERATIONS, rn_scale=RN_SCALE, summary_weight=SUMMARY_WEIGHT, n_derived=N_DERIVED,
+                outputs=OUTPUTS)
 
 
 def _bias_mask(widths):
