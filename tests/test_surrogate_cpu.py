@@ -97,8 +97,8 @@ def test_fit_follows_the_schedule_and_averages_the_last_epochs(epochs, average_l
 
 def test_load_refuses_a_model_for_other_targets(tmp_path):
     """Checked before any device memory is taken."""
-    meta = dict(sg._encoding(), persons=1000, widths=[len(sg.FEATURES) + sg.N_DERIVED, 8, sg.OUTPUTS], members=1, info={})
-    good = tmp_path / "good.npz"
+    meta = dict(sg._encoding(), persons=1000, widths=[len(sg.FEATURES) + sg.N_DERIVED, 8, sg.OUTPUTS], members=1,
+                info={})
     for key, value in (("summary_weight", sg.SUMMARY_WEIGHT + 1.0), ("days", sg.DAYS + 1),
                        ("ranges", dict(meta["ranges"], vaccination=[0.0, 0.9]))):
         bad = dict(meta, **{key: value})
@@ -108,7 +108,8 @@ def test_load_refuses_a_model_for_other_targets(tmp_path):
         with pytest.raises(ValueError, match=key):
             sg.Surrogate.load(path)
     wrong = dict(meta, widths=[3, 8, sg.OUTPUTS])
-    np.savez(good, params=np.zeros((1, 10), np.uint16), biases=np.zeros((1, 10), np.float32),
+    path = tmp_path / "bad_widths.npz"
+    np.savez(path, params=np.zeros((1, 10), np.uint16), biases=np.zeros((1, 10), np.float32),
              meta=np.array(json.dumps(wrong)))
     with pytest.raises(ValueError, match="widths"):
-        sg.Surrogate.load(good)
+        sg.Surrogate.load(path)
