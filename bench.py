@@ -378,7 +378,7 @@ def run_surrogate(args):
            "target": "<=5% relative error on peak height and attack rate; >=1000x scenarios/s"}
     seconds = {"test_data": t_test_sim}
     if os.path.exists(sg.SHIPPED_MODEL):
-        s = sg.Surrogate.load(sg.SHIPPED_MODEL)
+        s = sg.Surrogate.load(sg.SHIPPED_MODEL, max_batch=65536)   # chunks that fill the SMs
         pred, _ = s.predict(test)
         s.raw_features(X[:4096])
         t0 = time.time()

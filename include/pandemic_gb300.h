@@ -233,6 +233,9 @@ pt_status pt_mlp_train(pt_mlp *mlp, int epochs, int batch, float lr, uint64_t sh
 /* loss and the gradient of every parameter on n <= max_batch rows (no update) */
 pt_status pt_mlp_gradients(pt_mlp *mlp, const float *x, const float *y, int n, float *grads, float *loss);
 pt_status pt_mlp_predict(pt_mlp *mlp, const float *x, int n, float *y);
+/* the mean output of `count` networks of one shape on n rows (an ensemble): all run
+ * on the first network's stream, the mean is formed on the device and copied once */
+pt_status pt_mlp_predict_ensemble(pt_mlp *const *members, int count, const float *x, int n, float *y);
 void pt_mlp_destroy(pt_mlp *mlp);
 const char *pt_mlp_last_error(const pt_mlp *mlp);
 

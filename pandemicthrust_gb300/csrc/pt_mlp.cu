@@ -168,6 +168,13 @@ __global__ void k_gather(const float *X, const float *Y, const int *idx, int B, 
         for (int c = threadIdx.x; c < dout; c += blockDim.x) Yb[(long long)row * dout + c] = Y[src * dout + c];
 }
 
+// acc = (first ? 0 : acc) + scale * z over n values
+__global__ void k_accumulate(float *acc, const float *z, long long n, float scale, int first)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        acc[i] = first ? scale * z[i] : acc[i] + scale * z[i];
+}
+
 // mean squared error over B x dout; gradient of the output layer
 __global__ void k_mse(const float *Z, const float *Y, int B, int dout, float *dZf, bf16 *dZb, float *loss)
 {
@@ -548,6 +555,57 @@ pt_status pt_mlp_predict(pt_mlp *m, const float *X, int n, float *Y)
     if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
     cudaFree(dX);
     MCK(e, "predict");
+    return PT_OK;
+}
+
+pt_status pt_mlp_predict_ensemble(pt_mlp *const *members, int count, const float *X, int n, float *Y)
+{
+    if (!members || count < 1 || !X || !Y || n < 0) return PT_ERR_ARG;
+    pt_mlp *m = members[0];
+    if (!m) return PT_ERR_ARG;
+    int chunk = m->max_batch;
+    for (int j = 0; j < count; j++) {
+        pt_mlp *q = members[j];
+        if (!q) return PT_ERR_ARG;
+        if (q->L != m->L) return mfail(m, PT_ERR_ARG, "ensemble members differ in depth");
+        for (int l = 0; l <= m->L; l++)
+            if (q->width[l] != m->width[l]) return mfail(m, PT_ERR_ARG, "ensemble members differ in widths");
+        chunk = std::min(chunk, q->max_batch);
+    }
+    const int din = m->width[0], dout = m->width[m->L];
+    const cudaStream_t s = m->stream;
+    // every member runs on the first member's stream: finish what is queued on its own
+    for (int j = 1; j < count; j++)
+        if (members[j]->stream != s) MCK(cudaStreamSynchronize(members[j]->stream), "ensemble member stream");
+    float *dX = nullptr, *acc = nullptr;
+    const size_t rows = (size_t)std::max(1, std::min(n, chunk));
+    MCK(cudaMalloc(&dX, rows * din * sizeof(float)), "batch");
+    cudaError_t e = cudaMalloc(&acc, rows * dout * sizeof(float));
+    for (int s0 = 0; s0 < n && e == cudaSuccess; s0 += chunk) {
+        const int B = std::min(chunk, n - s0);
+        e = cudaMemcpyAsync(dX, X + (size_t)s0 * din, (size_t)B * din * sizeof(float), cudaMemcpyHostToDevice, s);
+        for (int j = 0; j < count && e == cudaSuccess; j++) {
+            pt_mlp *q = members[j];
+            const cudaStream_t own = q->stream;
+            q->stream = s;
+            k_gather<<<B, 128, 0, s>>>(dX, nullptr, nullptr, B, din, dout, q->H[0], nullptr);
+            e = forward(q, B);
+            if (e == cudaSuccess) {
+                const long long total = (long long)B * dout;
+                k_accumulate<<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, s>>>(
+                    acc, q->Z[q->L - 1], total, 1.0f / (float)count, j == 0);
+                e = cudaGetLastError();
+            }
+            q->stream = own;
+        }
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(Y + (size_t)s0 * dout, acc, (size_t)B * dout * sizeof(float), cudaMemcpyDeviceToHost,
+                                s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(dX);
+    if (acc) cudaFree(acc);
+    MCK(e, "ensemble predict");
     return PT_OK;
 }
 

@@ -64,6 +64,7 @@ class MLP:
         lib.pt_mlp_train.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_uint64, fp]
         lib.pt_mlp_gradients.argtypes = [vp, fp, fp, ctypes.c_int, fp, fp]
         lib.pt_mlp_predict.argtypes = [vp, fp, ctypes.c_int, fp]
+        lib.pt_mlp_predict_ensemble.argtypes = [ctypes.POINTER(vp), ctypes.c_int, fp, ctypes.c_int, fp]
         lib.pt_mlp_destroy.argtypes = [vp]
         lib.pt_mlp_last_error.argtypes = [vp]
         lib.pt_mlp_last_error.restype = ctypes.c_char_p
@@ -369,8 +370,14 @@ class Surrogate:
         return self.raw_features(features(scenarios))
 
     def raw_features(self, X):
-        """The same for rows of features() already computed."""
-        return np.mean([net.predict(X) for net in self.nets], axis=0)
+        """The same for rows of features() already computed.  The members' mean is
+        formed on the device (`pt_mlp_predict_ensemble`) and copied back once."""
+        X = np.ascontiguousarray(X, np.float32)
+        net0 = self.nets[0]
+        Y = np.zeros((len(X), net0.widths[-1]), np.float32)
+        members = (ctypes.c_void_p * len(self.nets))(*[net.h.value for net in self.nets])
+        net0._check(net0.lib.pt_mlp_predict_ensemble(members, len(self.nets), MLP._f(X), len(X), MLP._f(Y)))
+        return Y
 
     def predict(self, scenarios, fallback_replicates=4, seed_base=900_000):
         """Decoded predictions; scenarios outside the training ranges are simulated

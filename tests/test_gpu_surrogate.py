@@ -153,3 +153,13 @@ def test_shipped_surrogate_on_fresh_scenarios(native_lib):
     assert r["pairs"] >= 10
     assert r["peak_median"] < 0.08 and r["attack_median"] < 0.08, r
     assert r["peak_day_abs_median"] <= 3, r
+
+
+def test_ensemble_mean_on_device_matches_the_members(native_lib):
+    rng = np.random.default_rng(8)
+    s = sg.Surrogate(20_000, hidden=32, depth=2, seed=3, members=3, max_batch=64)
+    X = sg.features(sg.sample_scenarios(200, rng))   # more rows than max_batch: several chunks
+    want = np.mean([net.predict(X) for net in s.nets], axis=0)
+    np.testing.assert_allclose(s.raw_features(X), want, rtol=1e-5, atol=1e-6)
+    assert s.raw_features(X[:0]).shape == (0, sg.OUTPUTS)
+    s.close()
