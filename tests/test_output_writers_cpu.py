@@ -22,6 +22,13 @@ extern "C" int shim_rn(const char *path, const int *gp, const int *gs, int max_d
 { return pto::write_rn(path, gp, gs, max_days, persons) ? 0 : 1; }
 extern "C" int shim_max(const char *path, float proportion, int day)
 { return pto::write_infected_max(path, proportion, day) ? 0 : 1; }
+extern "C" int shim_profile(const char *path, int days, const int *infected, const float *ms8)
+{
+    std::vector<pto::ProfileRow> rows;
+    for (int d = 0; d < days; d++)
+        pto::day_profile_rows(rows, d, (d % 7) >= 5, 1000, infected[d], ms8 + 8 * d);
+    return pto::write_profile_log(path, rows) ? 0 : 1;
+}
 '''
 
 
@@ -38,6 +45,7 @@ def writers(tmp_path_factory):
     lib.shim_stats.argtypes = [ctypes.c_char_p, ip, ctypes.c_int]
     lib.shim_rn.argtypes = [ctypes.c_char_p, ip, ip, ctypes.c_int, ctypes.c_int]
     lib.shim_max.argtypes = [ctypes.c_char_p, ctypes.c_float, ctypes.c_int]
+    lib.shim_profile.argtypes = [ctypes.c_char_p, ctypes.c_int, ip, ctypes.POINTER(ctypes.c_float)]
     return lib
 
 
@@ -83,3 +91,34 @@ def test_writers_match_the_oracle_files(oracle_built, writers, tmp_path, params,
     assert writers.shim_max(str(mine / "infected_max.txt").encode(), float(best), best_day) == 0
     for name in ("output_infected_stats.csv", "output_rn.csv", "infected_max.txt"):
         assert (mine / name).read_bytes() == (ref / name).read_bytes(), name
+
+
+def test_profile_log_keeps_the_reference_profiler_format(writers, tmp_path):
+    """profiler.cu:13 (header) and :72-76 (rows: "%d, %d, %s, %d, %f, %lf"); children
+    are written before their parent; a day without infected ends after its first two
+    rows, as the reference breaks out of the loop there."""
+    import re
+    days = 8
+    infected = np.array([5, 9, 12, 20, 31, 40, 44, 0], np.int32)
+    ms = np.arange(days * 8, dtype=np.float32).reshape(days, 8) / 8.0
+    path = tmp_path / "profile_log.csv"
+    ip = infected.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    assert writers.shim_profile(str(path).encode(), days, ip, ms.ctypes.data_as(ctypes.POINTER(ctypes.c_float))) == 0
+    lines = path.read_text().splitlines()
+    assert lines[0] == ("day,stack_depth,function_name,problem_size,inclusive_time_milliseconds,"
+                        "exclusive_time_milliseconds")
+    rx = re.compile(r"^(\d+), (\d+), (\w+), (\d+), (\d+\.\d{6}), (\d+\.\d{6})$")
+    rows = [rx.match(l).groups() for l in lines[1:]]
+    by_day = {}
+    for r in rows:
+        by_day.setdefault(int(r[0]), []).append(r)
+    weekday = [r[2] for r in by_day[0]]
+    assert weekday == ["daily_countAndRecover", "daily_buildInfectedArray_global",
+                       "doWeekday_wholeDay_generateSchedulesKernel", "doWeekday_wholeDay_setup_sort",
+                       "doWeekday_wholeDay_setup_locationSearch", "doWeekday_wholeDay_kernel", "doWeekday_wholeDay"]
+    assert [r[2] for r in by_day[5]][-1] == "doWeekend_wholeDay"
+    assert [r[2] for r in by_day[7]] == ["daily_countAndRecover", "daily_buildInfectedArray_global"]
+    # the parent's inclusive time is its children's sum and its exclusive time zero
+    kids = sum(float(r[4]) for r in by_day[0][2:6])
+    assert abs(float(by_day[0][6][4]) - kids) < 1e-5 and float(by_day[0][6][5]) == 0.0
+    assert [int(r[1]) for r in by_day[0]] == [1, 1, 2, 2, 2, 2, 1]
