@@ -31,13 +31,13 @@ static inline void count_launch() { g_launches.fetch_add(1, std::memory_order_re
 
 int sm_count()
 {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0;
+    // initialised once, safely when several host threads drive engines
+    static const int n = [] {
+        int dev = 0, v = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 1;
-    }
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 1;
+    }();
     return n;
 }
 
