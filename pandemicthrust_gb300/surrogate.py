@@ -461,8 +461,16 @@ def _bf16_values(bits):
 def nearest_neighbour(train_X, train_Y, X):
     """The method without the network: each query takes the targets of the nearest
     training scenario in feature space."""
-    d = ((X[:, None, :] - train_X[None, :, :]) ** 2).sum(axis=2)
-    return train_Y[d.argmin(axis=1)]
+    T = np.asarray(train_X, np.float64)
+    Q = np.asarray(X, np.float64)
+    tn = (T * T).sum(axis=1)
+    best = np.empty(len(Q), np.int64)
+    step = max(1, (1 << 24) // max(len(T), 1))   # about 128 MB of distances at a time
+    for q0 in range(0, len(Q), step):
+        q = Q[q0:q0 + step]
+        # |q - t|^2 = |q|^2 - 2 q.t + |t|^2; |q|^2 does not change the argmin
+        best[q0:q0 + step] = (tn[None, :] - 2.0 * (q @ T.T)).argmin(axis=1)
+    return np.asarray(train_Y)[best]
 
 
 def evaluate(surrogate, scenarios, replicates, seed_base):

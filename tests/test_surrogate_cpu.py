@@ -113,3 +113,15 @@ def test_load_refuses_a_model_for_other_targets(tmp_path):
              meta=np.array(json.dumps(wrong)))
     with pytest.raises(ValueError, match="widths"):
         sg.Surrogate.load(path)
+
+
+def test_nearest_neighbour_matches_brute_force():
+    rng = np.random.default_rng(11)
+    T = rng.random((40000, 11)).astype(np.float32)   # enough rows that the queries go in several chunks
+    Y = np.arange(len(T))[:, None] * np.ones((1, 3))
+    X = rng.random((700, 11)).astype(np.float32)
+    want = np.concatenate([((X[i:i + 20, None, :].astype(np.float64) - T[None, :, :]) ** 2).sum(axis=2).argmin(axis=1)
+                           for i in range(0, len(X), 20)])
+    got = sg.nearest_neighbour(T, Y, X)[:, 0].astype(int)
+    # ties aside (none in random data), the same training row
+    np.testing.assert_array_equal(got, want)
