@@ -55,7 +55,7 @@ static const float kShedding[6][10] = {
 // roundHalfUp_toInt, PandemicSim.cu:1662-1665
 static int round_half_up(double d) { return (int)std::floor(d + 0.5); }
 
-pt_status derive(const pt_params &p, int core_seed, Derived &out, GlibcRand &rng, const char **why)
+pt_status derive(const pt_params &p, Derived &out, GlibcRand &rng, const char **why)
 {
     if (p.max_days < 0 || p.max_days > 255) {
         *why = "max_days must be in 0..255 (the reference's day counter is an 8-bit day_t)";

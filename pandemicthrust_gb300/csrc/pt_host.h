@@ -34,7 +34,7 @@ struct Derived {
 // Validates parameters and computes what PandemicSim's constructor derives from
 // them (setup_loadSeed, setup_scaleSimulation, setup_calculateInfectionData).
 // Returns PT_OK or PT_ERR_ARG with a message.
-pt_status derive(const pt_params &p, int core_seed, Derived &out, GlibcRand &rng, const char **why);
+pt_status derive(const pt_params &p, Derived &out, GlibcRand &rng, const char **why);
 
 // n_unique_numbers (PandemicSim.cu:1642-1659): n distinct rand() % max values.
 std::vector<int32_t> unique_numbers(GlibcRand &rng, int n, int max);

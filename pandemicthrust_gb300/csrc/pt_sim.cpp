@@ -162,7 +162,7 @@ static pt_status engine_create(Engine *s, const pt_params *params, const int *co
         in.core_seed = core_seeds[k];
         in.rng.reset(new pth::GlibcRand((unsigned int)in.core_seed));
         const char *why = nullptr;
-        pt_status st = pth::derive(in.params, in.core_seed, in.derived, *in.rng, &why);
+        pt_status st = pth::derive(in.params, in.derived, *in.rng, &why);
         if (st != PT_OK) {
             std::string m = why ? why : "invalid parameters";
             if (K > 1) m = "instance " + std::to_string(k) + ": " + m;
