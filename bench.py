@@ -17,8 +17,14 @@ e2e: the same metric through the C ABI from host buffers: pt_create -> pt_setup
 
 --impl reference times the reference's algorithm on the host cores: the CPU
 restatement in oracle/ (the reference's own host code covers only schedule
-regeneration, so it cannot run a day), one simulated day of the same 50M workload
-per step, on every host thread for the per-person stages.
+regeneration, so it cannot run a day), on every host thread for the per-person
+stages.  Its timed region is one whole 100-day run of the same 50M workload, cut into
+the requested number of steps of consecutive days.
+
+Parity evidence in the line (`parity`): the last timed 100-day run against the
+committed run of the reference's own kernels (tests/golden/headline_50M_100d.json),
+the first days against the oracle run by the CPU baseline, and every batched instance
+against the same instance run alone.
 
 Multi-GPU: replicas only (one independent simulation per rank, seed 777 + rank).
 """
@@ -181,27 +187,167 @@ def dist_setup():
     return world, rank, local
 
 
+STATE_FIELDS = ("status_p", "status_s", "day_p", "day_s", "gen_p", "gen_s")
+HEADLINE_GOLDEN = os.path.join(ROOT, "tests", "golden", "headline_50M_100d.json")
+
+
+def state_digests(state):
+    """SHA-256 of each per-person state array (equal digests: equal arrays)."""
+    import hashlib
+    import numpy as np
+    return {k: hashlib.sha256(np.ascontiguousarray(state[k]).tobytes()).hexdigest() for k in STATE_FIELDS}
+
+
 def cpu_sample(days, threads, params=PARAMS, seed=SEED):
-    """The oracle on the same 50M workload: setup (untimed), then `days` simulated days."""
+    """The oracle on the same 50M workload: setup (untimed), then `days` simulated days
+    (timed).  Also returns what the GPU's first days are checked against: each day's
+    16 bins, infected count and counter offset, and the digests of the per-person
+    state after the last day (recorded outside the timed region)."""
     from oracle import build_oracle
     from oracle.oracle import Oracle
     build_oracle.build()
     o = Oracle(params, seed, threads=threads)
     o.setup()
     N = o.view()["N"]
-    t0 = time.perf_counter()
+    dt = 0.0
     ran = 0
+    rows = []
     for _ in range(days):
-        rc, _, _ = o.step_day()
+        t0 = time.perf_counter()
+        rc, c, i = o.step_day()
+        dt += time.perf_counter() - t0
+        rows.append({"rc": rc, "counts": list(c), "infected": i, "rand_offset": o.view()["rand_offset"]})
         if rc != 0:
             break
         ran += 1
-    dt = time.perf_counter() - t0
+    record = {"rows": rows, "digests": state_digests(o.view())}
     o.close()
-    return N, ran, dt
+    return N, ran, dt, record
+
+
+def gpu_days(sim, days):
+    """The same days on the GPU through pt_step_day, from a reset of the resident
+    population: the record cpu_sample returns."""
+    sim.reset_epidemic()
+    rows = []
+    for _ in range(days):
+        rc, c, i = sim.step_day()
+        rows.append({"rc": rc, "counts": list(c), "infected": i, "rand_offset": sim.info()["rand_offset"]})
+        if rc != 0:
+            break
+    return {"rows": rows, "digests": state_digests(sim.person_state())}
+
+
+def parity_vs_oracle(gpu, cpu):
+    """Day-by-day comparison of the GPU's first days with the oracle's, exact."""
+    bad = []
+    if len(gpu["rows"]) != len(cpu["rows"]):
+        bad.append("days %d vs %d" % (len(gpu["rows"]), len(cpu["rows"])))
+    for d, (g, c) in enumerate(zip(gpu["rows"], cpu["rows"])):
+        for k in ("rc", "counts", "infected", "rand_offset"):
+            if g[k] != c[k]:
+                bad.append("day %d %s" % (d, k))
+    for k in STATE_FIELDS:
+        if gpu["digests"][k] != cpu["digests"][k]:
+            bad.append("final %s" % k)
+    return {"workload": WORKLOAD, "against": "oracle (C restatement), run in this bench", "days": len(cpu["rows"]),
+            "compared": "per-day 16 status bins, infected count, counter offset; SHA-256 of the six per-person "
+                        "state arrays after the last day",
+            "equal": not bad, "mismatches": bad[:8],
+            "final_state_sha256_prefix": {k: gpu["digests"][k][:16] for k in STATE_FIELDS}}
+
+
+def parity_vs_golden(counts, infected, digests, gen_p, gen_s, rand_offset):
+    """The timed 100-day runs against the committed run of the reference's own kernels
+    (compiled for the host, one thread: the canonical order) on the same workload."""
+    if not os.path.exists(HEADLINE_GOLDEN):
+        return None
+    with open(HEADLINE_GOLDEN) as fh:
+        g = json.load(fh)
+    bad = []
+    if len(g["days"]) != len(infected):
+        bad.append("days %d vs %d" % (len(infected), len(g["days"])))
+    for d, ref in enumerate(g["days"][:len(infected)]):
+        if [int(x) for x in counts[d]] != ref["counts"]:
+            bad.append("day %d counts" % d)
+        if int(infected[d]) != ref["infected"]:
+            bad.append("day %d infected" % d)
+    if g["days"] and int(rand_offset) != g["days"][-1]["rand_offset"]:
+        bad.append("final rand_offset")
+    for k in STATE_FIELDS:
+        if digests[k] != g["final"][k]:
+            bad.append("final %s" % k)
+    if [int(x) for x in gen_p] != g["gen_p"] or [int(x) for x in gen_s] != g["gen_s"]:
+        bad.append("generation counts")
+    return {"workload": WORKLOAD, "against": "the reference's kernels compiled for the host "
+                                             "(tests/golden/headline_50M_100d.json, tests/golden/make_golden.py)",
+            "days": len(g["days"]),
+            "compared": "every day's 16 status bins and infected count of each timed run's last step; final "
+                        "counter offset, SHA-256 of the six per-person state arrays, generation counts",
+            "equal": not bad, "mismatches": bad[:8]}
+
+
+def cpu_model():
+    """Host CPU model and core count, for the CPU baseline's record."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() in ("Model name", "Model"):
+                name = line.split(":", 1)[1].strip()
+                if not name.isdigit():
+                    break
+    except Exception:
+        pass
+    return {"model": name, "nproc": os.cpu_count()}
+
+
+# Single-thread oracle figures (the reference's CPU path has no engine of its own that
+# runs a day): the 100,000-person x 30-day workload and a 1M-person run shaped like
+# the 50M one (same location ratio, R, seeds).
+SINGLE_THREAD_WORKLOADS = {
+    "c1_100k_persons_30_days": (dict(max_days=30, r_pandemic=1.4, r_seasonal=1.2, initial_pandemic=10,
+                                     initial_seasonal=10, people_scaling=0.04248, location_scaling=0.04248,
+                                     percent_symptomatic=1.0, asymp_factor=0.0), 12345),
+    "c2_shape_1M_persons_30_days": (dict(max_days=30, r_pandemic=1.5, r_seasonal=1.2, initial_pandemic=100,
+                                         initial_seasonal=100, people_scaling=0.42481, location_scaling=4.2481,
+                                         percent_symptomatic=1.0, asymp_factor=0.0), 777),
+}
+
+
+def single_thread_baselines():
+    from oracle.oracle import Oracle
+    out = {}
+    for name, (p, seed) in SINGLE_THREAD_WORKLOADS.items():
+        o = Oracle(p, seed, threads=1)
+        o.setup()
+        N = o.view()["N"]
+        t0 = time.perf_counter()
+        days = 0
+        for _ in range(p["max_days"]):
+            rc, _, _ = o.step_day()
+            if rc == 2:
+                break
+            days += 1
+            if rc == 1:
+                break
+        dt = time.perf_counter() - t0
+        o.close()
+        out[name] = {"value": N * days / dt, "unit": UNIT, "persons": N, "days": days, "seconds": dt, "cores": 1}
+    return out
+
+
+def workload_config(N, H, L, max_days):
+    """The `config` object both arms print: the workload, not the hardware."""
+    return {"workload": WORKLOAD, "persons": N, "households": H, "locations": L, "days": max_days,
+            "l2": "inputs larger than L2 (about 4 GB of per-person state)"}
 
 
 def run_reference(args, world, rank):
+    """The reference's algorithm on the host cores (the oracle restatement, every host
+    thread on the per-person stages).  The timed region is one whole 100-day run of
+    the workload, cut into `steps` steps of ceil(100 / steps) consecutive days; the
+    warm-up steps run the same days on a separate copy of the population first."""
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
@@ -210,30 +356,46 @@ def run_reference(args, world, rank):
     build_oracle.build()
     params = dict(PARAMS)
     params["people_scaling"] = PARAMS["people_scaling"] * args.scale
+    params["location_scaling"] = PARAMS["location_scaling"] * args.scale
+    max_days = params["max_days"]
+    per = max(1, -(-max_days // max(args.steps, 1)))
+
+    def steps_of(o, nsteps):
+        dt, days = 0.0, 0
+        for _ in range(nsteps):
+            t0 = time.perf_counter()
+            for _ in range(per):
+                rc, _, _ = o.step_day()
+                if rc == 2:
+                    break
+                days += 1
+                if rc == 1:
+                    break
+            dt += time.perf_counter() - t0
+        return dt, days
+
     o = Oracle(params, SEED, threads=threads)
     o.setup()
-    N = o.view()["N"]
-    for _ in range(args.warmup):
-        o.step_day()
-    t0 = time.perf_counter()
-    ran = 0
-    for _ in range(args.steps):
-        rc, _, _ = o.step_day()
-        if rc == 0:
-            ran += 1
-    dt = time.perf_counter() - t0
+    steps_of(o, min(args.warmup, -(-max_days // per)))
     o.close()
-    value = N * ran / dt
+    o = Oracle(params, SEED, threads=threads)
+    o.setup()
+    v = o.view()
+    N, H, L = v["N"], v["H"], v["L"]
+    dt, days = steps_of(o, args.steps)
+    o.close()
+    value = N * days / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / max(args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/i32/f32",
         "data": "synthetic (the reference's generator, seed 777)",
-        "config": {"workload": WORKLOAD, "persons": N, "days_per_step": 1, "parallelism": "host threads",
-                   "l2": "inputs larger than L2"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "%d persons, days %d-%d after %d warm-up days, setup excluded" %
-                                   (N, args.warmup, args.warmup + args.steps - 1, args.warmup)},
+        "config": workload_config(N, H, L, max_days),
+        "parallelism": "%d host threads" % threads,
+        "days_per_step": per, "days_simulated": days,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "host": cpu_model(),
+                         "sample": "%d persons, days 0-%d of one run (%d per step), setup excluded; %d warm-up "
+                                   "steps on a separate copy" % (N, days - 1, per, args.warmup)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -273,6 +435,13 @@ def run_batched(args, pt, torch, stream, local):
     ms = t0.elapsed_time(t1)
     value = person_days / (ms / 1000.0)
     days = b.days_run()
+    # each instance's results of the last timed step (read after the timed region),
+    # for the comparison with the same instance run alone below
+    bgp, bgs = b.final_gen_counts()
+    batch_results = []
+    for k in range(K):
+        c, i = b.counts(k)
+        batch_results.append((c, i, bgp[k], bgs[k], state_digests(b.person_state(k))))
     # stage breakdown: one more run with per-stage CUDA events (outside the timed region)
     b.set_timing(True)
     b.reset_epidemic()
@@ -305,7 +474,10 @@ def run_batched(args, pt, torch, stream, local):
     # warm-up run, so its day loop is already a captured graph)
     plain_ms = 0.0
     plain_pd = 0
-    for p, sd in zip(params, seeds):
+    identical = 0
+    differing = []
+    import numpy as np
+    for k, (p, sd) in enumerate(zip(params, seeds)):
         sim = pt.PandemicSim(p, sd, stream=sp)
         sim.setupSim()
         sim.runToCompletion()
@@ -314,11 +486,20 @@ def run_batched(args, pt, torch, stream, local):
         a0 = torch.cuda.Event(enable_timing=True)
         a1 = torch.cuda.Event(enable_timing=True)
         a0.record(stream)
-        _, inf = sim.runToCompletion()
+        cnt, inf = sim.runToCompletion()
         a1.record(stream)
         torch.cuda.synchronize()
         plain_ms += a0.elapsed_time(a1)
         plain_pd += sim.info()["number_people"] * len(inf)
+        # bit-identity of instance k with its run alone
+        gp, gs = sim.final_gen_counts()
+        c, i, bgp_k, bgs_k, dig = batch_results[k]
+        same = (np.array_equal(c, cnt) and np.array_equal(i, inf) and np.array_equal(bgp_k, gp) and
+                np.array_equal(bgs_k, gs) and dig == state_digests(sim.person_state()))
+        if same:
+            identical += 1
+        else:
+            differing.append(k)
         sim.close()
     plain_value = plain_pd / (plain_ms / 1000.0)
     return {
@@ -334,6 +515,11 @@ def run_batched(args, pt, torch, stream, local):
         "plain_sequential": {"value": plain_value, "unit": UNIT, "ms": plain_ms,
                              "note": "each instance alone through the plain path, device time of its run"},
         "speedup_vs_plain_sequential": value / plain_value,
+        "parity": {"instances": K, "bit_identical_instances": identical, "equal": identical == K,
+                   "differing_instances": differing[:16],
+                   "compared": "each instance of the batch against the same parameters and seed run alone "
+                               "through the plain path: every statistics row, generation counts, SHA-256 of "
+                               "the six per-person state arrays"},
         "config": "persons log-uniform in [2e5, 4e6], R per strain uniform in [1.1, 2.0], 10 + 10 seeds, "
                   "seed 1000 + k, inputs larger than L2",
         "clocks": clocks,
@@ -504,6 +690,13 @@ def main():
     else:
         person_days = float(N) * days_total
     value = person_days / (ms / 1000.0)
+    # parity of the last timed step (read after the timed region) against the
+    # committed run of the reference's own kernels on the same workload
+    golden = None
+    if rank == 0 and args.scale == 1.0 and seed == SEED:
+        gp, gs = sim.final_gen_counts()
+        golden = parity_vs_golden(counts, infected, state_digests(sim.person_state()), gp, gs,
+                                  sim.info()["rand_offset"])
 
     # stage breakdown: one more step with per-stage CUDA events (outside the timed region)
     sim.set_timing(True)
@@ -540,6 +733,9 @@ def main():
     traffic = ncu_traffic().get(dominant)
     all_bytes = sum(day_bytes(d % 7 >= 5, N, L, int(infected[d])) for d in range(days))
     day_achieved = all_bytes / (run_ms / 1000.0) / 1e9
+
+    # the first days again through pt_step_day, for the comparison with the oracle
+    gpu_first_days = gpu_days(sim, args.cpu_days) if (rank == 0 and world == 1 and not args.no_cpu) else None
 
     # e2e: whole pipeline through the C ABI from host buffers
     e2e_value = None
@@ -578,12 +774,15 @@ def main():
         surrogate = run_surrogate(args)
 
     cpu = None
+    oracle_parity = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        cN, cdays, cdt = cpu_sample(args.cpu_days, threads)
-        cpu = {"value": cN * cdays / cdt, "unit": UNIT, "cores": threads, "kind": "port",
+        cN, cdays, cdt, record = cpu_sample(args.cpu_days, threads, params, seed)
+        oracle_parity = parity_vs_oracle(gpu_first_days, record)
+        cpu = {"value": cN * cdays / cdt, "unit": UNIT, "cores": threads, "kind": "port", "host": cpu_model(),
                "sample": "oracle (C restatement) on the same %d-person workload, days 0-%d (setup excluded), "
-                         "%d host threads" % (cN, cdays - 1, threads)}
+                         "%d host threads" % (cN, cdays - 1, threads),
+               "single_thread": single_thread_baselines()}
 
     if rank == 0:
         line = {
@@ -591,10 +790,12 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8/i32/f32",
             "data": "synthetic (the reference's population generator, seed 777 + rank)",
-            "config": {"workload": WORKLOAD, "persons": N, "households": info["number_households"],
-                       "locations": L, "days_per_step": days_total / args.steps,
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "inputs larger than L2 (about 4 GB of per-person state)"},
+            "config": workload_config(N, info["number_households"], L, params["max_days"]),
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "days_per_step": days_total / args.steps,
+            "parity": {"plain_50M_vs_reference_kernels_100_days": golden,
+                       "plain_50M_vs_oracle_first_days": oracle_parity,
+                       "batched_instances_vs_alone": batched.get("parity") if batched else None},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,

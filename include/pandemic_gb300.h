@@ -181,6 +181,19 @@ pt_status pt_get_stage_ms(pt_sim *sim, float ms[16], int days[2]);
  * timed).  The drop-in executable writes them as the reference's profile_log.csv. */
 pt_status pt_get_day_stage_ms(pt_sim *sim, int day, float ms[8]);
 
+/* Checks the error path of the library's device-side waits (no counterpart in the
+ * reference, whose kernel errors go unchecked, PandemicSim.cu:2754-2761).  Every wait
+ * of one thread block for another (the decoupled look-backs of the scans and sorts)
+ * gives up after a bounded number of polls, records an error word and returns, and
+ * the host then reports PT_ERR_TIMEOUT with the device still usable.  This runs that
+ * same wait code in one small kernel, waiting for a predecessor's prefix: with
+ * publish_predecessor != 0 the prefix is written first and the call returns PT_OK
+ * with *prefix = 1234; with 0 nothing ever writes it, the wait gives up after
+ * spin_limit polls and the call returns PT_ERR_TIMEOUT (text in pt_last_error(NULL)).
+ * spin_limit must lie in [0, 2^22], the limit the simulation's own waits use, else
+ * PT_ERR_ARG.  Allocates and frees 64 bytes of device memory; synchronises the device. */
+pt_status pt_selftest_bounded_wait(int publish_predecessor, int64_t spin_limit, uint32_t *prefix);
+
 /* Kernel launches issued by this library in the calling process so far. */
 uint64_t pt_launch_count(void);
 
@@ -188,7 +201,9 @@ uint64_t pt_launch_count(void);
 pt_status pt_transfer_bytes(const pt_sim *sim, uint64_t *h2d, uint64_t *d2h);
 
 /* Largest input pt_bucket_table_static accepts: its scratch space is compiled into
- * the library, about 21 MiB of device memory held by every GPU that loads it. */
+ * the library, about 21 MiB of device memory, committed on a device when the
+ * library's device code first loads there (its first call, or the first kernel any
+ * entry point launches) and held until the process exits. */
 #define PT_STATIC_TABLE_MAX_ENTRIES (1 << 20)
 #define PT_STATIC_TABLE_MAX_BUCKETS (1 << 20)
 
@@ -204,10 +219,13 @@ pt_status pt_transfer_bytes(const pt_sim *sim, uint64_t *h2d, uint64_t *d2h);
  * offsets[buckets] = n.  The same table pt_setup builds for workplaces.
  * n <= PT_STATIC_TABLE_MAX_ENTRIES and buckets <= PT_STATIC_TABLE_MAX_BUCKETS, else
  * PT_ERR_ARG; a key outside [0, buckets) also gives PT_ERR_ARG.  Work runs on
- * cuda_stream (NULL: the default stream) and the call returns once the table is
- * complete.  The first call on a device looks up the scratch's device address; make
- * that first call before any stream capture.  All calls share one scratch area, so
- * calls that overlap on the GPU race with each other: do not overlap them. */
+ * cuda_stream (NULL: the default stream); the call synchronises that stream and
+ * returns once the table is complete.  The first call on a device looks up the
+ * scratch's device address; make that first call before any stream capture, and
+ * make it at initialisation when a memory pool will later claim the device's
+ * budget.  The address is kept: do not use the library across a cudaDeviceReset.
+ * All calls share one scratch area, so calls that overlap on the GPU race with each
+ * other: do not overlap them. */
 pt_status pt_bucket_table_static(const int32_t *keys, int n, int buckets, int32_t *offsets,
                                  int32_t *table, void *cuda_stream);
 

@@ -20,7 +20,9 @@ import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF_ROOT = os.environ.get("PT_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: PT_REFERENCE_ROOT, else a directory named "reference" beside
+# this repository's root.
+REF_ROOT = os.environ.get("PT_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 SRC_DIR = os.path.join(REF_ROOT, "PandemicThrust", "PandemicThrust")
 R123_DIR = os.path.join(REF_ROOT, "PandemicThrust", "Random123")
 

@@ -21,6 +21,7 @@ __all__ = ["PandemicSim", "PandemicBatch", "Params", "Interventions", "load_libr
            "CLI_PATH", "BATCH_CLI_PATH", "PT_OK", "PT_DONE", "PT_FINISHED"]
 
 PT_OK, PT_DONE, PT_FINISHED = 0, 1, 2
+PT_ERR_ARG, PT_ERR_IO, PT_ERR_PARSE, PT_ERR_OOM, PT_ERR_CUDA, PT_ERR_STATE, PT_ERR_TIMEOUT = -1, -2, -3, -4, -5, -6, -7
 _STATUS = {0: "PT_OK", 1: "PT_DONE", 2: "PT_FINISHED", -1: "PT_ERR_ARG", -2: "PT_ERR_IO", -3: "PT_ERR_PARSE",
            -4: "PT_ERR_OOM", -5: "PT_ERR_CUDA", -6: "PT_ERR_STATE", -7: "PT_ERR_TIMEOUT"}
 

@@ -1746,6 +1746,38 @@ cudaError_t launch_apply(const DevArrays &d, int day, cudaStream_t s)
     return cudaGetLastError();
 }
 
+// ================================================================== bounded-wait probe
+// The look-back wait above, in isolation: one warp plays tile 1 of a fresh look-back
+// (epoch 1, words zeroed by the host) and waits for tile 0.  With publish_first the
+// warp writes tile 0's inclusive prefix (1234) before waiting, and the wait returns it
+// at once.  Without it nothing ever writes tile 0's word: the wait polls spin_limit
+// times, records the error word and returns, and the kernel ends normally.
+__global__ void k_wait_probe(LookBack lb, int publish_first, long long spin_limit, unsigned *prefix_out)
+{
+    constexpr unsigned kEpoch = 1;
+    if (publish_first && threadIdx.x == 0) {
+        *(volatile unsigned long long *)&lb.tiles[0] = lb_word(kEpoch, 2, 1234u);
+        __threadfence();
+    }
+    __syncwarp();
+    const unsigned excl = lookback_publish_warp(lb, kEpoch, 1, 5u, false, spin_limit);
+    if (threadIdx.x == 0) *prefix_out = excl;
+}
+
+cudaError_t launch_wait_probe(unsigned long long *tiles, int *error, int publish_first, long long spin_limit,
+                              unsigned *prefix_out, cudaStream_t s)
+{
+    LookBack lb;
+    lb.tiles = tiles;
+    lb.ctl = nullptr;   // the probe takes no ticket
+    lb.error = error;
+    k_wait_probe<<<1, 32, 0, s>>>(lb, publish_first, spin_limit, prefix_out);
+    count_launch();
+    return cudaGetLastError();
+}
+
+long long max_spin_limit() { return kSpinLimit; }
+
 // ================================================================== final
 // final_countReproduction's generation counts (PandemicSim.cu:2227-2304) for every
 // instance: one block per person tile, histogram in shared memory.

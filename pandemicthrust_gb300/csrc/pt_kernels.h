@@ -202,6 +202,11 @@ int day_buckets(const SimConst &c, bool weekend);
 // ---- final: per-instance generation histograms, K x 512 (pandemic 0..255, seasonal 256..511)
 cudaError_t launch_gen_hist(const DevArrays &d, int *hist, cudaStream_t s);
 
+// ---- the bounded look-back wait in isolation (tiles: 2 zeroed words; error: zeroed)
+cudaError_t launch_wait_probe(unsigned long long *tiles, int *error, int publish_first, long long spin_limit,
+                              unsigned *prefix_out, cudaStream_t s);
+long long max_spin_limit();   // the polls every wait of the simulation allows
+
 uint64_t launches();
 void add_launches(int64_t n);  // kernels run by a replayed graph
 

@@ -30,9 +30,10 @@ __device__ __forceinline__ unsigned long long lb_word(unsigned epoch, unsigned f
 // 32 predecessors per step (one word per lane) to the nearest inclusive prefix,
 // publishes the tile's inclusive prefix and returns the exclusive one on every lane.
 // A tile that starts a segment (segment_start) publishes its aggregate as its
-// inclusive prefix: the scans of consecutive segments are independent.
+// inclusive prefix: the scans of consecutive segments are independent.  After
+// spin_limit polls without progress the wait records lb.error and gives up.
 static __device__ unsigned lookback_publish_warp(const LookBack &lb, unsigned epoch, int tile, unsigned aggregate,
-                                                 bool segment_start = false)
+                                                 bool segment_start = false, long long spin_limit = kSpinLimit)
 {
     volatile unsigned long long *t = lb.tiles;
     const int lane = threadIdx.x & 31;
@@ -63,7 +64,7 @@ static __device__ unsigned lookback_publish_warp(const LookBack &lb, unsigned ep
             top -= 32;
             continue;
         }
-        if (++spins > kSpinLimit) {
+        if (++spins > spin_limit) {
             if (lane == 0) atomicExch(lb.error, 1);
             break;
         }

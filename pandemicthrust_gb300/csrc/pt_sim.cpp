@@ -1004,6 +1004,35 @@ pt_status pt_transfer_bytes(const pt_sim *s, uint64_t *h2d, uint64_t *d2h)
     return PT_OK;
 }
 
+pt_status pt_selftest_bounded_wait(int publish_predecessor, int64_t spin_limit, uint32_t *prefix)
+{
+    if (spin_limit < 0 || spin_limit > ptk::max_spin_limit()) {
+        g_create_error = "spin_limit outside [0, the simulation's own limit]";
+        return PT_ERR_ARG;
+    }
+    // two look-back words, the error word and the returned prefix, all zero
+    void *mem = nullptr;
+    cudaError_t e = cudaMalloc(&mem, 64);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc(probe)");
+    unsigned long long *tiles = (unsigned long long *)mem;
+    int *error = (int *)(tiles + 2);
+    unsigned *out = (unsigned *)(error + 1);
+    int h_error = 0;
+    unsigned h_prefix = 0;
+    e = cudaMemset(mem, 0, 64);
+    if (e == cudaSuccess) e = ptk::launch_wait_probe(tiles, error, publish_predecessor ? 1 : 0, spin_limit, out, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(&h_error, error, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&h_prefix, out, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    cudaFree(mem);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "bounded-wait probe");
+    if (prefix) *prefix = h_prefix;
+    if (h_error) {
+        g_create_error = "a device-side wait gave up (bounded-wait probe)";
+        return PT_ERR_TIMEOUT;
+    }
+    return PT_OK;
+}
+
 void pt_destroy(pt_sim *s) { delete s; }
 
 const char *pt_last_error(const pt_sim *s)

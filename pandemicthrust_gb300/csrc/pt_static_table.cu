@@ -8,10 +8,16 @@
 // and errand tables (person ids grouped by key, ascending within each key, with
 // offsets) using only scratch space compiled into the library: the array below.
 //
-// The array is fixed at load time and every GPU that loads the library holds it
-// until the process exits.  All calls share it and it keeps the last call's
+// The array is part of the library's device code.  With lazy module loading (the
+// CUDA default) its memory is committed when the module first loads on a device: at
+// the first call, or at the first kernel any entry point of the library launches
+// there.  From then on that GPU holds it until the process exits.  A caller whose
+// pool claims the whole device budget should make one call at initialisation,
+// before carving the pool.  All calls share the array and it keeps the last call's
 // contents, so two calls that overlap on the GPU (on different streams, or from
 // different host threads) race and corrupt each other's tables: serialise them.
+// The device address is looked up once per device and kept; the library must not be
+// used across a cudaDeviceReset.
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -26,6 +32,8 @@ namespace {
 constexpr int kMaxEntries = PT_STATIC_TABLE_MAX_ENTRIES;
 constexpr int kMaxBuckets = PT_STATIC_TABLE_MAX_BUCKETS;
 constexpr int kTile = 4096;                                      // radix and scan tile
+static_assert(kTile == ptk::kRadixTileEntries && kTile == ptk::kScanTileEntries,
+              "the scratch layout sizes the look-back words by the kernels' tile sizes");
 constexpr int kRadixTiles = (kMaxEntries + kTile - 1) / kTile;
 constexpr int kScanTiles = (kMaxBuckets + 1 + kTile - 1) / kTile + 4;
 

@@ -8,7 +8,8 @@ oracle/build_ref.py (the reference tree must be present, so run this where it is
   * whole runs of the reference's kernels (one-thread grid, canonical order):
     per-day status bins, infected counts, generation counts and state digests.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py              rng.json, regen.json, runs.json
+    python tests/golden/make_golden.py --headline   headline_50M_100d.json
 """
 import hashlib
 import json
@@ -130,9 +131,47 @@ def run_digest(params, seed):
     return dict(params=params, seed=seed, setup=setup, days=days, gen_p=gp.tolist(), gen_s=gs.tolist())
 
 
+# The headline workload: 50M persons x 100 days (people_scaling 21.24044, location
+# scaling 10x that, R 1.5 / 1.2, 100 + 100 seeds, seed 777).  Too large for per-day
+# state digests, so it records every day's bins, infected count and counter, and the
+# digests of the setup tables and of the final per-person state.
+HEADLINE = (make_params(max_days=100, r_pandemic=1.5, r_seasonal=1.2, initial_pandemic=100, initial_seasonal=100,
+                        people_scaling=21.24044, location_scaling=212.4044), 777)
+
+
+def headline_digest(params, seed):
+    sim = RefSim(params, seed)
+    sim.setup()
+    v0 = sim.view()
+    setup = dict(N=v0["N"], H=v0["H"], L=v0["L"], adults=v0["adults"], children=v0["children"],
+                 rand_offset=v0["rand_offset"], age=digest(v0["age"]), household=digest(v0["household"]),
+                 workplace=digest(v0["workplace"]), workplace_people=digest(v0["workplace_people"]),
+                 workplace_offset=digest(v0["workplace_offset"]))
+    days = []
+    while True:
+        rc, counts, infected = sim.step_day()
+        if rc == 2:
+            break
+        days.append(dict(rc=rc, counts=counts, infected=infected, rand_offset=sim.view()["rand_offset"]))
+        print("day", len(days) - 1, infected, flush=True)
+        if rc == 1:
+            break
+    v = sim.view()
+    final = {k: digest(v[k]) for k in ("status_p", "status_s", "day_p", "day_s", "gen_p", "gen_s")}
+    gp, gs = sim.gen_counts()
+    sim.close()
+    return dict(params=params, seed=seed, setup=setup, days=days, final=final, gen_p=gp.tolist(),
+                gen_s=gs.tolist())
+
+
 def main():
     if build_ref.build() is None:
         raise SystemExit("the reference tree is needed to generate golden fixtures")
+    if "--headline" in sys.argv:
+        # about 40 minutes on one host core: the reference kernels run one thread
+        with open(os.path.join(HERE, "headline_50M_100d.json"), "w") as fh:
+            json.dump(headline_digest(*HEADLINE), fh)
+        return
     with open(os.path.join(HERE, "rng.json"), "w") as fh:
         json.dump(rng_vectors(), fh)
     with open(os.path.join(HERE, "regen.json"), "w") as fh:

@@ -21,3 +21,24 @@ def test_reference_arm_prints_one_contract_line():
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["cores"] >= 1
     assert d["config"]["persons"] > 10_000 and "workload" in d["config"]
+    assert d["days_simulated"] == 100 and d["days_per_step"] == 50
+
+
+def test_parity_helpers_flag_a_planted_difference():
+    # the comparisons bench.py reports: equal records pass, one changed field fails
+    sys.path.insert(0, ROOT)
+    import bench
+    import numpy as np
+    rows = [{"rc": 0, "counts": list(range(16)), "infected": 5, "rand_offset": 100 + d} for d in range(3)]
+    state = {k: np.arange(10, dtype=np.uint8) for k in bench.STATE_FIELDS}
+    rec = {"rows": rows, "digests": bench.state_digests(state)}
+    same = bench.parity_vs_oracle(rec, json.loads(json.dumps(rec)))
+    assert same["equal"] and same["days"] == 3
+    planted = json.loads(json.dumps(rec))
+    planted["rows"][1]["rand_offset"] += 1
+    bad = bench.parity_vs_oracle(rec, planted)
+    assert not bad["equal"] and bad["mismatches"] == ["day 1 rand_offset"]
+    state2 = dict(state, gen_s=state["gen_s"].copy())
+    state2["gen_s"][3] ^= 1
+    bad = bench.parity_vs_oracle(rec, {"rows": rows, "digests": bench.state_digests(state2)})
+    assert bad["mismatches"] == ["final gen_s"]

@@ -36,12 +36,16 @@ def test_static_table_equals_setup_workplace_table_twice(native_lib):
     N, L = info["number_people"], info["number_workplaces"]
     assert N <= (1 << 20)
     keys = torch.from_numpy(pop["workplace"]).cuda()
-    for _ in range(2):
+    for call in range(2):
         offsets = torch.full((L + 1,), -7, dtype=torch.int32, device="cuda")
         table = torch.full((N,), -7, dtype=torch.int32, device="cuda")
         torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         rc = build_table(keys.data_ptr(), N, L, offsets.data_ptr(), table.data_ptr(), None)
+        free_after = torch.cuda.mem_get_info()[0]
         assert rc == 0
+        if call == 1:  # after the first call has loaded the scratch: no device memory taken
+            assert free_after == free_before
         assert np.array_equal(offsets.cpu().numpy(), pop["workplace_offset"])
         assert np.array_equal(table.cpu().numpy(), pop["workplace_people"])
 
