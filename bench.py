@@ -262,8 +262,11 @@ def parity_vs_golden(counts, infected, digests, gen_p, gen_s, rand_offset):
     (compiled for the host, one thread: the canonical order) on the same workload."""
     if not os.path.exists(HEADLINE_GOLDEN):
         return None
-    with open(HEADLINE_GOLDEN) as fh:
-        g = json.load(fh)
+    try:
+        with open(HEADLINE_GOLDEN) as fh:
+            g = json.load(fh)
+    except ValueError as e:
+        return {"workload": WORKLOAD, "equal": False, "mismatches": ["unreadable golden fixture: %s" % e]}
     bad = []
     if len(g["days"]) != len(infected):
         bad.append("days %d vs %d" % (len(infected), len(g["days"])))

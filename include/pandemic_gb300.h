@@ -181,6 +181,28 @@ pt_status pt_get_stage_ms(pt_sim *sim, float ms[16], int days[2]);
  * timed).  The drop-in executable writes them as the reference's profile_log.csv. */
 pt_status pt_get_day_stage_ms(pt_sim *sim, int day, float ms[8]);
 
+/* Launch shapes of the day's kernels.  The reference fixes its grids per device at
+ * compile time (device_K20.h:4-8: 32 blocks of 256 threads); here they are chosen at
+ * run time, by the caller or by pt_autotune.  Every choice gives bit-identical
+ * results; only the speed differs. */
+typedef struct pt_tuning {
+    int infect_coop;            /* 0: one thread per infector; 1: eight lanes per infector */
+    int infect_blocks_per_sm;   /* infection grid, 256-thread blocks per SM: 1..32 */
+    int radix_blocks_per_sm;    /* persistent blocks of a day's radix pass per SM: 1..3 */
+} pt_tuning;
+
+/* Sets / reads the launch shapes of sim (allowed before or after pt_setup). */
+pt_status pt_set_tuning(pt_sim *sim, const pt_tuning *t);
+pt_status pt_get_tuning(const pt_sim *sim, pt_tuning *t);
+
+/* The tuner: after pt_setup, runs the first `days` days (0: all of max_days) once
+ * per candidate launch shape with per-stage CUDA events, keeps the fastest shape for
+ * the infection stage and for the radix stage (each is timed on its own stage), sets
+ * it, and resets the epidemic.  Results of later runs do not depend on the choice.
+ * A shape found for an engine of the same size (instances, persons, bucket counts,
+ * SM count) earlier in the process is reused without timing.  chosen may be NULL. */
+pt_status pt_autotune(pt_sim *sim, int days, pt_tuning *chosen);
+
 /* Checks the error path of the library's device-side waits (no counterpart in the
  * reference, whose kernel errors go unchecked, PandemicSim.cu:2754-2761).  Every wait
  * of one thread block for another (the decoupled look-backs of the scans and sorts)
@@ -320,6 +342,11 @@ pt_status pt_batch_set_timing(pt_batch *batch, int enabled);
 pt_status pt_batch_get_stage_ms(pt_batch *batch, float ms[16], int days[2]);
 
 pt_status pt_batch_transfer_bytes(const pt_batch *batch, uint64_t *h2d, uint64_t *d2h);
+
+/* As pt_set_tuning / pt_get_tuning / pt_autotune, for the batch. */
+pt_status pt_batch_set_tuning(pt_batch *batch, const pt_tuning *t);
+pt_status pt_batch_get_tuning(const pt_batch *batch, pt_tuning *t);
+pt_status pt_batch_autotune(pt_batch *batch, int days, pt_tuning *chosen);
 
 void pt_batch_destroy(pt_batch *batch);
 

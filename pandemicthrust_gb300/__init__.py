@@ -72,6 +72,22 @@ class Interventions(ctypes.Structure):
         return iv
 
 
+class Tuning(ctypes.Structure):
+    """Launch shapes of the day's kernels (pt_tuning); every choice gives identical results."""
+    _fields_ = [("infect_coop", ctypes.c_int), ("infect_blocks_per_sm", ctypes.c_int),
+                ("radix_blocks_per_sm", ctypes.c_int)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+    @classmethod
+    def from_dict(cls, d):
+        t = cls()
+        for name, _ in cls._fields_:
+            setattr(t, name, int(d[name]))
+        return t
+
+
 class Info(ctypes.Structure):
     _fields_ = [
         ("number_people", ctypes.c_int), ("number_households", ctypes.c_int),
@@ -97,6 +113,8 @@ EXPORTS = [
     "pt_batch_size", "pt_batch_counts", "pt_batch_final_gen_counts", "pt_batch_get_info",
     "pt_batch_get_person_state", "pt_batch_get_population", "pt_batch_set_timing", "pt_batch_get_stage_ms",
     "pt_batch_transfer_bytes", "pt_batch_destroy", "pt_batch_last_error",
+    "pt_set_tuning", "pt_get_tuning", "pt_autotune", "pt_batch_set_tuning", "pt_batch_get_tuning",
+    "pt_batch_autotune", "pt_selftest_bounded_wait", "pt_bucket_table_static",
 ]
 
 _lib = None
@@ -135,6 +153,12 @@ def load_library(path=None):
     lib.pt_get_day_stage_ms.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
     lib.pt_set_interventions.argtypes = [vp, ctypes.POINTER(Interventions)]
     lib.pt_batch_set_interventions.argtypes = [vp, ctypes.POINTER(Interventions)]
+    tp = ctypes.POINTER(Tuning)
+    for pre in ("pt_", "pt_batch_"):
+        getattr(lib, pre + "set_tuning").argtypes = [vp, tp]
+        getattr(lib, pre + "get_tuning").argtypes = [vp, tp]
+        getattr(lib, pre + "autotune").argtypes = [vp, ctypes.c_int, tp]
+    lib.pt_selftest_bounded_wait.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint32)]
     lib.pt_launch_count.restype = ctypes.c_uint64
     lib.pt_launch_count.argtypes = []
     lib.pt_transfer_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
@@ -266,6 +290,22 @@ class PandemicSim:
 
     def set_timing(self, on=True):
         self._check(self.lib.pt_set_timing(self.h, 1 if on else 0))
+
+    def set_tuning(self, t):
+        """Launch shapes (a dict or Tuning): infect_coop, infect_blocks_per_sm, radix_blocks_per_sm."""
+        t = Tuning.from_dict(t) if isinstance(t, dict) else t
+        self._check(self.lib.pt_set_tuning(self.h, ctypes.byref(t)))
+
+    def tuning(self):
+        t = Tuning()
+        self._check(self.lib.pt_get_tuning(self.h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def autotune(self, days=0):
+        """Times the candidate launch shapes on the first `days` days (0: all), keeps the fastest."""
+        t = Tuning()
+        self._check(self.lib.pt_autotune(self.h, int(days), ctypes.byref(t)))
+        return t.as_dict()
 
     STAGES = ("sweep", "infected_list", "schedule", "digit_bases", "bucket_sort", "bucket_offsets", "infect", "apply")
 
@@ -413,6 +453,20 @@ class PandemicBatch:
 
     def set_timing(self, on=True):
         self._check(self.lib.pt_batch_set_timing(self.h, 1 if on else 0))
+
+    def set_tuning(self, t):
+        t = Tuning.from_dict(t) if isinstance(t, dict) else t
+        self._check(self.lib.pt_batch_set_tuning(self.h, ctypes.byref(t)))
+
+    def tuning(self):
+        t = Tuning()
+        self._check(self.lib.pt_batch_get_tuning(self.h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def autotune(self, days=0):
+        t = Tuning()
+        self._check(self.lib.pt_batch_autotune(self.h, int(days), ctypes.byref(t)))
+        return t.as_dict()
 
     def stage_ms(self):
         a = (ctypes.c_float * 16)()

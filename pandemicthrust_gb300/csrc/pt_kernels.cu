@@ -561,7 +561,8 @@ cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
     const int P = radix_passes(r.buckets);
     const int bits = key_bits(r.buckets);
     const int tiles = std::max(1, div_up(r.E, kRadixTile));
-    const int grid = std::max(1, std::min(tiles, 3 * sm_count()));  // persistent blocks
+    const int bps = std::max(1, std::min(3, r.blocks_per_sm));
+    const int grid = std::max(1, std::min(tiles, bps * sm_count()));  // persistent blocks
     const uint32_t *kin = r.keys;
     const uint32_t *vin = r.vals;   // nullptr: implicit values (entry index -> person)
     const bool implicit = r.vals == nullptr;
@@ -700,6 +701,38 @@ cudaError_t launch_seed_infected(const int32_t *seeds, int P, int S, uint32_t *s
 {
     if (P + S <= 0) return cudaSuccess;
     k_seed_infected<<<div_up(P + S, 256), 256, 0, s>>>(seeds, P, S, state, gen_p, gen_s);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// The packed per-person records (PersonRec layout in pt_kernels.h): one thread per
+// person.  Everything in a record is fixed once the workplace table exists.
+__global__ void k_person_records(const InstConst *ic, const int32_t *tile_inst, int P, const int32_t *household,
+                                 const int32_t *hh_offset, const int32_t *workplace, const int32_t *wp_offset,
+                                 const uint8_t *age, uint4 *prec)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+        const int hh = household[p];
+        if (hh < 0) {  // padding person
+            prec[p] = make_uint4(0u, 0u, 0u, 0u);
+            continue;
+        }
+        const InstConst &k = ic[tile_inst[p / kPersonTile]];
+        const int hoff = hh_offset[hh], hcnt = hh_offset[hh + 1] - hoff;
+        const int wp = workplace[p];
+        const int woff = wp_offset[wp], wcnt = wp_offset[wp + 1] - woff;
+        const int loc = wp - k.lbase;
+        const uint32_t w = (uint32_t)hcnt | ((uint32_t)age[p] << 4) | ((uint32_t)workplace_max_contacts(k.c, loc) << 8) |
+                           ((uint32_t)is_school(k.c, loc) << 10);
+        prec[p] = make_uint4((uint32_t)hoff, (uint32_t)woff, (uint32_t)wcnt, w);
+    }
+}
+
+cudaError_t launch_person_records(const DevArrays &d, cudaStream_t s)
+{
+    const int blocks = std::max(1, std::min(div_up(d.P, 256), sm_count() * 16));
+    k_person_records<<<blocks, 256, 0, s>>>(d.ic, d.tile_inst, d.P, d.household, d.hh_offset, d.workplace,
+                                            d.wp_offset, d.age, d.prec);
     count_launch();
     return cudaGetLastError();
 }
@@ -1341,6 +1374,7 @@ static RadixArgs day_radix_args(const DevArrays &d, bool weekend)
     r.error = &d.sc->error;
     r.skip = &d.sc->done;
     r.keep_keys = true;  // the bucket offsets come from the sorted keys
+    r.blocks_per_sm = d.tune.radix_blocks_per_sm;
     return r;
 }
 
@@ -1538,14 +1572,19 @@ struct InfectArgs {
     const InstState *is;
     const uint32_t *state;
     const uint8_t *gen_p, *gen_s, *age;
-    const int32_t *household, *hh_offset, *workplace, *wp_people, *wp_offset;
+    const uint4 *prec;
+    const int32_t *wp_people;
     const int32_t *keys, *bkt_offset, *bkt_people, *infected, *infected_inst;
     unsigned long long *claim;
     int32_t *new_list;
     Scalars *sc;
 };
 
-// kernel_doWeekday + device_makeContacts_weekday (PandemicSim.cu:3236-3308, :1669-1829)
+// An infector's packed record: one 128-bit read-only load.
+__device__ __forceinline__ uint4 load_record(const uint4 *prec, int me) { return __ldg(&prec[me]); }
+
+// kernel_doWeekday + device_makeContacts_weekday (PandemicSim.cu:3236-3308, :1669-1829),
+// one thread per infector.
 __global__ void __launch_bounds__(128) k_infect_weekday(InfectArgs a, int day)
 {
     Scalars *sc = a.sc;
@@ -1563,25 +1602,23 @@ __global__ void __launch_bounds__(128) k_infect_weekday(InfectArgs a, int day)
         const int me = inf.me;
         const int lme = me - ik.pbase;  // the instance's person number
         const unsigned long long ctr = s.infect_offset + 6ull * (unsigned long long)(pos - s.start);
+        const uint4 rec = load_record(a.prec, me);
         uint32_t w[8];
         tf2x64(key, ctr, w);
         tf2x64(key, ctr + 1, w + 4);
-        const int age = a.age[me];
-        const bool adult = age == 5;
+        const bool adult = prec_age(rec.w) == 5;
         int victims[8], kv[8];
         int ksum = 0;
         // household: offset + r % count, the household table is the identity
-        const int hh = a.household[me];
-        const int hoff = a.hh_offset[hh], hcnt = a.hh_offset[hh + 1] - hoff;
+        const int hoff = (int)rec.x, hcnt = prec_household_size(rec.w);
 #pragma unroll
         for (int j = 0; j < 3; j++) {
             kv[j] = select_victim(me, hoff, hcnt, w[j], true, nullptr, victims[j]);
             ksum += kv[j];
         }
         // workplace or school: max-contacts of its type
-        const int wp = a.workplace[me];
-        const int woff = a.wp_offset[wp], wcnt = a.wp_offset[wp + 1] - woff;
-        const int desired = workplace_max_contacts(c, wp - ik.lbase);
+        const int woff = (int)rec.y, wcnt = (int)rec.z;
+        const int desired = prec_desired(rec.w);
         // errands / afterschool: destinations from today's keys; the adult
         // profile is regenerated from the schedule counter (:3667-3705)
         const int32_t *kk = a.keys + ik.kbase;
@@ -1612,7 +1649,7 @@ __global__ void __launch_bounds__(128) k_infect_weekday(InfectArgs a, int day)
         // contacts; they keep their share of ksum, so the contact does not happen
         // rather than passing its weight to the others
         if (desired > 0 && (ik.absent_thr != 0 || (day >= ik.closure_start && day < ik.closure_end))) {
-            const bool closed = day >= ik.closure_start && day < ik.closure_end && is_school(c, wp - ik.lbase);
+            const bool closed = day >= ik.closure_start && day < ik.closure_end && prec_school(rec.w);
             const bool me_absent =
                 adult && intervention_hash(c.key0, c.key1, kTagAbsent, day, lme) < ik.absent_thr;
 #pragma unroll
@@ -1666,12 +1703,12 @@ __global__ void __launch_bounds__(128) k_infect_weekend(InfectArgs a, int day)
         const int me = inf.me;
         const int lme = me - ik.pbase;
         const unsigned long long ctr = s.infect_offset + 6ull * (unsigned long long)(pos - s.start);
+        const uint4 rec = load_record(a.prec, me);
         uint32_t w[4];
         tf2x64(key, ctr, w);
         int victims[5], kv[5];
         int ksum = 0;
-        const int hh = a.household[me];
-        const int hoff = a.hh_offset[hh], hcnt = a.hh_offset[hh + 1] - hoff;
+        const int hoff = (int)rec.x, hcnt = prec_household_size(rec.w);
 #pragma unroll
         for (int j = 0; j < 3; j++) {
             kv[j] = select_victim(me, hoff, hcnt, w[j], true, nullptr, victims[j]);
@@ -1694,19 +1731,189 @@ __global__ void __launch_bounds__(128) k_infect_weekend(InfectArgs a, int day)
     }
 }
 
+// ---------------------------------------------------- warp-cooperative contacts
+// The same draws with eight lanes per infector (four infectors per warp round).  Lane
+// j of a group first computes one Threefry block of the infector's draws, all in
+// parallel:
+//   weekday  j = 0, 1: contact words (counters R + 6 pos, +1); j = 2..5: infection
+//            words (+2..+5); j = 6: the schedule block of the adult's errand profile
+//   weekend  j = 0: contact words; j = 1: the Threefry-2x32 errand block; j = 2..5:
+//            infection words
+// then picks contact slot j's victim (its own gather chain) and draws slot j's two
+// infections.  The words reach the lanes that use them by shuffles; the contact sum
+// is a shuffle reduction over the group.  Every draw, victim and claim key equals the
+// one-thread-per-infector kernels' (same counters, same words, same slots).
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ uint32_t pick4(int i, uint32_t q0, uint32_t q1, uint32_t q2, uint32_t q3)
+{
+    return i == 0 ? q0 : (i == 1 ? q1 : (i == 2 ? q2 : q3));
+}
+
+// Slot j's infection draws: words W[2j], W[2j+1], W[(2j+2) & 15] of the four
+// infection blocks, which lanes 2..5 of the group hold.
+__device__ __forceinline__ void infection_words(const uint32_t blk[4], int gl, int j, uint32_t &w0, uint32_t &w1,
+                                                uint32_t &w2)
+{
+    const int sa = gl + 2 + (j >> 1), sb = gl + 2 + (((j + 1) & 7) >> 1);
+    const uint32_t a0 = __shfl_sync(kFull, blk[0], sa), a1 = __shfl_sync(kFull, blk[1], sa);
+    const uint32_t a2 = __shfl_sync(kFull, blk[2], sa), a3 = __shfl_sync(kFull, blk[3], sa);
+    const uint32_t b0 = __shfl_sync(kFull, blk[0], sb), b2 = __shfl_sync(kFull, blk[2], sb);
+    w0 = (j & 1) ? a2 : a0;
+    w1 = (j & 1) ? a3 : a1;
+    w2 = ((j + 1) & 1) ? b2 : b0;
+}
+
+// Slot j's two infection draws against its victim (process_contacts for one slot).
+__device__ __forceinline__ void claim_slot(const SimConst &c, const InfectArgs &a, int pos, int j, int me, int victim,
+                                           int kv, const float prob[2], uint32_t w0, uint32_t w1, uint32_t w2)
+{
+    const float kf = __int2float_rn(kv);
+#pragma unroll
+    for (int strain = 0; strain < 2; strain++) {
+        const float y = to_unit(strain ? w1 : w0);
+        if (y < __fmul_rn(prob[strain], kf)) {
+            const uint32_t st = a.state[victim];
+            const uint32_t vstatus = strain ? ((st >> 8) & 0xFFu) : (st & 0xFFu);
+            if (vstatus == 1u) {
+                const int profile = infection_profile(c, strain ? (w1 ^ w2) : (w0 ^ w1));
+                const int gen = ((strain ? a.gen_s[me] : a.gen_p[me]) + 1) & 0xFF;
+                const unsigned long long k = ((unsigned long long)((long long)pos * 8 + j) << 16) |
+                                             ((unsigned long long)profile << 8) | (unsigned long long)gen;
+                const unsigned long long old = atomicMin(&a.claim[2 * (size_t)victim + strain], k);
+                if (old == ~0ull) a.new_list[atomicAdd(&a.sc->new_count, 1)] = 2 * victim + strain;
+            }
+        }
+    }
+}
+
+// Infection probability of each strain (device_calculateInfectionProbability); -1
+// when the strain is not infectious today.
+__device__ __forceinline__ void infector_probs(const SimConst &c, uint32_t st, int day, int ksum, float prob[2])
+{
+#pragma unroll
+    for (int strain = 0; strain < 2; strain++) {
+        const uint32_t status = strain ? ((st >> 8) & 0xFFu) : (st & 0xFFu);
+        const uint32_t dday = strain ? (st >> 24) : ((st >> 16) & 0xFFu);
+        prob[strain] = -1.f;
+        if (status >= 2u) {
+            const int pd = day - (int)dday;
+            if (pd >= 0 && pd < 10) prob[strain] = infection_probability(c, (int)status - 2, pd, strain, ksum);
+        }
+    }
+}
+
+template <bool WEEKEND>
+__global__ void __launch_bounds__(256) k_infect_coop(InfectArgs a, int day)
+{
+    Scalars *sc = a.sc;
+    if (sc->done) return;
+    const int I = sc->infected;
+    const int lane = threadIdx.x & 31, j = lane & 7, gl = lane & ~7;
+    const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int base = gwarp * 4; base < I; base += nwarps * 4) {   // warp-uniform
+        const int pos0 = base + (lane >> 3);
+        const bool act = pos0 < I;       // groups past the list's end shadow its last entry
+        const int pos = act ? pos0 : I - 1;
+        const int inst = a.infected_inst[pos];
+        const InstConst &ik = a.ic[inst];
+        const SimConst &c = ik.c;
+        const InstState &s = a.is[inst];
+        const int me = a.infected[pos];
+        const int lme = me - ik.pbase;
+        const unsigned long long ctr = s.infect_offset + 6ull * (unsigned long long)(pos - s.start);
+        const TfKey key = make_key(c);
+        const uint4 rec = load_record(a.prec, me);
+        // one Threefry block per lane
+        uint32_t blk[4] = {0u, 0u, 0u, 0u};
+        if (WEEKEND && j == 1) {
+            tf2x32(key, (uint32_t)(ctr + 1), blk);   // :1895-1901, counter truncated to 32 bits
+        } else {
+            const uint64_t cc = (!WEEKEND && j >= 6) ? s.errand_offset + (uint64_t)(lme / 2) : ctr + (uint64_t)j;
+            tf2x64(key, cc, blk);
+        }
+        // contact words: W[j] of blocks R, R + 1 (weekday), W[j] of block R (weekend)
+        const int csrc = WEEKEND ? gl : gl + (j >> 2);
+        const uint32_t q0 = __shfl_sync(kFull, blk[0], csrc), q1 = __shfl_sync(kFull, blk[1], csrc);
+        const uint32_t q2 = __shfl_sync(kFull, blk[2], csrc), q3 = __shfl_sync(kFull, blk[3], csrc);
+        const uint32_t wc = pick4(j & 3, q0, q1, q2, q3);
+        int victim = -1, kv = 0;
+        const int hoff = (int)rec.x, hcnt = prec_household_size(rec.w);
+        if (WEEKEND) {
+            const int prof = (int)(q3 % 6u);   // word 3 of block R (:1892)
+            const uint32_t v0 = __shfl_sync(kFull, blk[0], gl + 1), v1 = __shfl_sync(kFull, blk[1], gl + 1);
+            if (j < 3) {
+                kv = select_victim(me, hoff, hcnt, wc, true, nullptr, victim);
+            } else if (j < 5) {
+                const int loc = a.keys[ik.kbase + 3 * (size_t)lme + c_weekend_assign[prof][j - 3]];
+                const int eoff = a.bkt_offset[loc], ecnt = a.bkt_offset[loc + 1] - eoff;
+                kv = select_victim(me, eoff, ecnt, j == 3 ? v0 : v1, false, a.bkt_people, victim);
+            }
+        } else {
+            const bool adult = prec_age(rec.w) == 5;
+            const int desired = prec_desired(rec.w);
+            // the adult's errand profile from the schedule block on lane 6 (:3697-3702)
+            const int pv = (j == 6) ? (int)(((lme & 1) ? (blk[2] ^ blk[3]) : (blk[0] ^ blk[1])) % 3u) : 0;
+            const int prof = adult ? __shfl_sync(kFull, pv, gl + 6) : 3;
+            if (j < 3) {
+                kv = select_victim(me, hoff, hcnt, wc, true, nullptr, victim);
+            } else if (j < 3 + desired) {
+                kv = select_victim(me, (int)rec.y, (int)rec.z, wc, false, a.wp_people, victim);
+            } else {
+                const int e = j - 3 - desired, want0 = c_weekday_assign[prof][0], want1 = c_weekday_assign[prof][1];
+                const int hour = e < want0 ? 0 : (e < want0 + want1 ? 1 : -1);
+                if (hour >= 0) {
+                    const int dest = a.keys[ik.kbase + (size_t)hour * c.N + lme];
+                    const int eoff = a.bkt_offset[dest], ecnt = a.bkt_offset[dest + 1] - eoff;
+                    kv = select_victim(me, eoff, ecnt, wc, false, a.bkt_people, victim);
+                }
+            }
+        }
+        // the contact sum over the group's slots
+        int ksum = kv;
+        ksum += __shfl_xor_sync(kFull, ksum, 4);
+        ksum += __shfl_xor_sync(kFull, ksum, 2);
+        ksum += __shfl_xor_sync(kFull, ksum, 1);
+        if (!WEEKEND && j >= 3 && j < 3 + prec_desired(rec.w) && kv != 0 &&
+            (ik.absent_thr != 0 || (day >= ik.closure_start && day < ik.closure_end))) {
+            // interventions void a workplace / school contact after it counted in ksum
+            const bool closed = day >= ik.closure_start && day < ik.closure_end && prec_school(rec.w);
+            const bool me_absent = prec_age(rec.w) == 5 &&
+                                   intervention_hash(c.key0, c.key1, kTagAbsent, day, lme) < ik.absent_thr;
+            const bool v_absent = ik.absent_thr != 0 && a.age[victim] == 5 &&
+                                  intervention_hash(c.key0, c.key1, kTagAbsent, day, victim - ik.pbase) <
+                                      ik.absent_thr;
+            if (closed || me_absent || v_absent) kv = 0;
+        }
+        float prob[2];
+        infector_probs(c, a.state[me], day, ksum, prob);
+        uint32_t w0, w1, w2;
+        infection_words(blk, gl, j, w0, w1, w2);
+        if (act && kv != 0 && j < (WEEKEND ? 5 : 8)) claim_slot(c, a, pos, j, me, victim, kv, prob, w0, w1, w2);
+    }
+}
+
 cudaError_t launch_infect(const DevArrays &d, bool weekend, int day, cudaStream_t s)
 {
     InfectArgs a;
     a.ic = d.ic; a.is = d.is;
     a.state = d.state; a.gen_p = d.gen_p; a.gen_s = d.gen_s; a.age = d.age;
-    a.household = d.household; a.hh_offset = d.hh_offset; a.workplace = d.workplace;
-    a.wp_people = d.wp_people; a.wp_offset = d.wp_offset; a.keys = d.keys;
+    a.prec = d.prec;
+    a.wp_people = d.wp_people; a.keys = d.keys;
     a.bkt_offset = d.bkt_offset; a.bkt_people = d.bkt_people; a.infected = d.infected;
     a.infected_inst = d.infected_inst;
     a.claim = d.claim; a.new_list = d.new_list; a.sc = d.sc;
-    int blocks = sm_count() * 16;
-    if (weekend) k_infect_weekend<<<blocks, 128, 0, s>>>(a, day);
-    else k_infect_weekday<<<blocks, 128, 0, s>>>(a, day);
+    const Tuning &t = d.tune;
+    if (t.infect_coop) {
+        const int blocks = sm_count() * t.infect_blocks_per_sm;
+        if (weekend) k_infect_coop<true><<<blocks, 256, 0, s>>>(a, day);
+        else k_infect_coop<false><<<blocks, 256, 0, s>>>(a, day);
+    } else {
+        const int blocks = sm_count() * t.infect_blocks_per_sm * 2;   // blocks of 128 threads
+        if (weekend) k_infect_weekend<<<blocks, 128, 0, s>>>(a, day);
+        else k_infect_weekday<<<blocks, 128, 0, s>>>(a, day);
+    }
     count_launch();
     return cudaGetLastError();
 }

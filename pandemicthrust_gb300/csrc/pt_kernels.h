@@ -81,6 +81,15 @@ struct Scalars {
     int pad;
 };
 
+// Launch shapes chosen at run time (the engine's tuner picks them per engine; every
+// choice gives bit-identical results, only the speed differs).
+struct Tuning {
+    int infect_coop = 0;            // 1: warp-cooperative contacts (8 lanes per infector)
+    int infect_blocks_per_sm = 8;   // infection grid: 256-thread blocks per SM (twice as
+                                    // many 128-thread blocks for the thread-per-infector kernels)
+    int radix_blocks_per_sm = 3;    // persistent blocks of a day's radix pass per SM (1..3)
+};
+
 // Device pointers of a batch of simulations (one simulation is a batch of one).
 // Person, household, location and bucket ids are global: an instance's ids are its
 // local ids plus its bases.
@@ -93,6 +102,7 @@ struct DevArrays {
     int32_t *workplace;       // P
     int32_t *wp_people;       // P (padding persons last, in the spare bucket)
     int32_t *wp_offset;       // locations + 2
+    uint4 *prec;              // P packed per-person records for the contact draws (see PersonRec)
     int32_t *keys;            // 3P schedule keys (global bucket indices)
     int32_t *bkt_offset;      // buckets (each instance's buckets and its end slot)
     int32_t *bkt_count;       // buckets histogram, zero between uses
@@ -121,7 +131,22 @@ struct DevArrays {
     int bucket_max[2];        // largest weekday / weekend bucket count of one instance
     int locations;            // locations over all instances
     Scalars *sc;
+    Tuning tune;
 };
+
+// The static part of a person that the contact draws read, packed in 16 bytes so an
+// infector's own data is one 128-bit load (built once at setup, after the workplace
+// table):
+//   x  first person of the person's household (household victims are x + r % size)
+//   y  start of the person's workplace / school in the workplace table
+//   z  persons in that workplace / school
+//   w  bits 0-3 household size, 4-7 age code, 8-9 workplace contacts (the type's
+//      maximum, PandemicSim.cu:3492-3511), bit 10 the location is a school (types 3-7)
+// Padding persons have an all-zero record (they are never infected).
+__host__ __device__ inline int prec_household_size(uint32_t w) { return (int)(w & 15u); }
+__host__ __device__ inline int prec_age(uint32_t w) { return (int)((w >> 4) & 15u); }
+__host__ __device__ inline int prec_desired(uint32_t w) { return (int)((w >> 8) & 3u); }
+__host__ __device__ inline bool prec_school(uint32_t w) { return ((w >> 10) & 1u) != 0; }
 
 // Launch configuration helpers
 int sm_count();
@@ -170,6 +195,7 @@ struct RadixArgs {
     int *ctl;                     // ticket, finished, epoch
     int *error;
     const int *skip;
+    int blocks_per_sm = 3;        // persistent blocks per SM (1..3, the kernel's occupancy bound)
 };
 int radix_passes(int buckets);
 cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s);
@@ -186,6 +212,8 @@ cudaError_t launch_reset_instances(const DevArrays &d, cudaStream_t s);
 cudaError_t launch_vaccinate(const DevArrays &d, cudaStream_t s);
 cudaError_t launch_seed_infected(const int32_t *seeds, int P, int S, uint32_t *state, uint8_t *gen_p,
                                  uint8_t *gen_s, cudaStream_t s);
+// the packed per-person records (after households, workplaces and the workplace table)
+cudaError_t launch_person_records(const DevArrays &d, cudaStream_t s);
 
 // ---- day (every instance of the batch in each launch)
 cudaError_t launch_sweep(const DevArrays &d, int day, cudaStream_t s);          // recover, count, scan, bookkeeping

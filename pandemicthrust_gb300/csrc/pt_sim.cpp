@@ -11,7 +11,9 @@
 #include <climits>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -367,6 +369,7 @@ static pt_status engine_setup(Engine *s)
     bytes += round256(n * 4);                   // state
     bytes += 3 * round256(n);                   // gen_p, gen_s, age
     bytes += round256(n * 4) * 3;               // household, workplace, wp_people
+    bytes += round256(n * 16);                  // packed person records
     bytes += round256(((size_t)LT + 2) * 4);    // wp_offset
     bytes += round256(3 * n * 4) * 6;           // keys, bkt_people, radix k0/v0/k1/v1
     bytes += round256(((size_t)Bday + 1) * 4);  // bkt_offset
@@ -393,6 +396,7 @@ static pt_status engine_setup(Engine *s)
     d.workplace = a.take<int32_t>(n);
     d.wp_people = a.take<int32_t>(n);
     d.wp_offset = a.take<int32_t>((size_t)LT + 2);
+    d.prec = a.take<uint4>(n);
     d.keys = a.take<int32_t>(3 * n);
     d.bkt_people = a.take<int32_t>(3 * n);
     d.rk0 = a.take<uint32_t>(3 * n);
@@ -457,6 +461,7 @@ static pt_status engine_setup(Engine *s)
         CK(ptk::launch_bucket_table(r, d.bkt_count, true, d.wp_offset, d.tiles, ctl, d.digit_hist, s->stream),
            "workplace table");
     }
+    CK(ptk::launch_person_records(d, s->stream), "person records");
     // initial infected: rand() % N draws continue each instance's seed sequence
     // (PandemicSim.cu:708-758); the first P of an instance get the pandemic strain
     s->seed_global.clear();
@@ -825,6 +830,115 @@ static pt_status engine_stage_ms(Engine *s, float ms[16], int days[2])
     return PT_OK;
 }
 
+// ------------------------------------------------------------------ launch shapes
+static pt_tuning to_public(const ptk::Tuning &t)
+{
+    pt_tuning o;
+    o.infect_coop = t.infect_coop;
+    o.infect_blocks_per_sm = t.infect_blocks_per_sm;
+    o.radix_blocks_per_sm = t.radix_blocks_per_sm;
+    return o;
+}
+
+static pt_status engine_set_tuning(Engine *s, const pt_tuning *t)
+{
+    if (!t || (t->infect_coop != 0 && t->infect_coop != 1) || t->infect_blocks_per_sm < 1 ||
+        t->infect_blocks_per_sm > 32 || t->radix_blocks_per_sm < 1 || t->radix_blocks_per_sm > 3)
+        return fail(s, PT_ERR_ARG, "launch shape outside its range");
+    ptk::Tuning n;
+    n.infect_coop = t->infect_coop;
+    n.infect_blocks_per_sm = t->infect_blocks_per_sm;
+    n.radix_blocks_per_sm = t->radix_blocks_per_sm;
+    if (n.infect_coop != s->d.tune.infect_coop || n.infect_blocks_per_sm != s->d.tune.infect_blocks_per_sm ||
+        n.radix_blocks_per_sm != s->d.tune.radix_blocks_per_sm) {
+        // the captured day loop holds the old launch shapes
+        if (s->stream) cudaStreamSynchronize(s->stream);
+        if (s->run_graph) cudaGraphExecDestroy(s->run_graph);
+        s->run_graph = nullptr;
+    }
+    s->d.tune = n;
+    return PT_OK;
+}
+
+// Shapes already chosen in this process, by engine size.
+static std::mutex g_tune_mutex;
+static std::map<std::vector<long long>, pt_tuning> g_tune_cache;
+
+static std::vector<long long> tune_key(const Engine *s)
+{
+    return {s->K(), s->d.P, s->d.bucket_max[0], s->d.bucket_max[1], s->d.buckets[0], s->d.buckets[1],
+            s->max_days, ptk::sm_count()};
+}
+
+// The tuner.  The infection stage and the radix stage are timed separately (per-stage
+// CUDA events around every day), so one run measures one candidate of each: run i
+// uses infection candidate i and radix candidate i % 3.
+static pt_status engine_autotune(Engine *s, int days, pt_tuning *chosen)
+{
+    if (!s->setup_done) return fail(s, PT_ERR_STATE, "autotune before setup");
+    if (days < 0) return fail(s, PT_ERR_ARG, "negative day count");
+    const std::vector<long long> key = tune_key(s);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            pt_status st = engine_set_tuning(s, &it->second);
+            if (st == PT_OK && chosen) *chosen = it->second;
+            return st;
+        }
+    }
+    struct Cand { int coop, bps; };
+    // thread-per-infector kernel: 9 resident 128-thread blocks per SM at 56 registers;
+    // warp-cooperative kernel: 6 resident 256-thread blocks per SM at 40 registers
+    const Cand infect[] = {{0, 8}, {0, 4}, {1, 6}, {1, 12}, {1, 3}, {0, 16}};
+    const int radix[] = {3, 2, 1};
+    const int runs = (int)(sizeof(infect) / sizeof(infect[0]));
+    float best_inf = 1e30f, best_rad[3] = {1e30f, 1e30f, 1e30f};
+    int best_i = 0;
+    const int saved_max = s->max_days;
+    const int trial = days > 0 ? std::min(days, saved_max) : saved_max;
+    for (int i = 0; i < runs; i++) {
+        pt_tuning t;
+        t.infect_coop = infect[i].coop;
+        t.infect_blocks_per_sm = infect[i].bps;
+        t.radix_blocks_per_sm = radix[i % 3];
+        pt_status st = engine_set_tuning(s, &t);
+        if (st == PT_OK) st = engine_reset(s);
+        if (st == PT_OK) st = engine_set_timing(s, 1);
+        if (st != PT_OK) return st;
+        s->max_days = trial;
+        st = engine_run(s);
+        s->max_days = saved_max;
+        if (st != PT_OK) return st;
+        float ms[16];
+        engine_stage_ms(s, ms, nullptr);
+        const float inf = ms[kStInfect] + ms[8 + kStInfect];
+        const float rad = ms[kStRadix] + ms[8 + kStRadix];
+        if (inf < best_inf) {
+            best_inf = inf;
+            best_i = i;
+        }
+        best_rad[i % 3] = std::min(best_rad[i % 3], rad);
+    }
+    int rbest = 0;
+    for (int r = 1; r < 3; r++)
+        if (best_rad[r] < best_rad[rbest]) rbest = r;
+    pt_tuning t;
+    t.infect_coop = infect[best_i].coop;
+    t.infect_blocks_per_sm = infect[best_i].bps;
+    t.radix_blocks_per_sm = radix[rbest];
+    pt_status st = engine_set_timing(s, 0);
+    if (st == PT_OK) st = engine_set_tuning(s, &t);
+    if (st == PT_OK) st = engine_reset(s);
+    if (st != PT_OK) return st;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tune_cache[key] = t;
+    }
+    if (chosen) *chosen = t;
+    return PT_OK;
+}
+
 extern "C" {
 
 // ------------------------------------------------------------------ one simulation
@@ -977,6 +1091,25 @@ pt_status pt_set_timing(pt_sim *s, int enabled)
 {
     if (!s) return PT_ERR_ARG;
     return engine_set_timing(s, enabled);
+}
+
+pt_status pt_set_tuning(pt_sim *s, const pt_tuning *t)
+{
+    if (!s || !t) return PT_ERR_ARG;
+    return engine_set_tuning(s, t);
+}
+
+pt_status pt_get_tuning(const pt_sim *s, pt_tuning *t)
+{
+    if (!s || !t) return PT_ERR_ARG;
+    *t = to_public(s->d.tune);
+    return PT_OK;
+}
+
+pt_status pt_autotune(pt_sim *s, int days, pt_tuning *chosen)
+{
+    if (!s) return PT_ERR_ARG;
+    return engine_autotune(s, days, chosen);
 }
 
 pt_status pt_get_stage_ms(pt_sim *s, float ms[16], int days[2])
@@ -1145,6 +1278,25 @@ pt_status pt_batch_set_timing(pt_batch *b, int enabled)
 {
     if (!b) return PT_ERR_ARG;
     return engine_set_timing(b, enabled);
+}
+
+pt_status pt_batch_set_tuning(pt_batch *b, const pt_tuning *t)
+{
+    if (!b || !t) return PT_ERR_ARG;
+    return engine_set_tuning(b, t);
+}
+
+pt_status pt_batch_get_tuning(const pt_batch *b, pt_tuning *t)
+{
+    if (!b || !t) return PT_ERR_ARG;
+    *t = to_public(b->d.tune);
+    return PT_OK;
+}
+
+pt_status pt_batch_autotune(pt_batch *b, int days, pt_tuning *chosen)
+{
+    if (!b) return PT_ERR_ARG;
+    return engine_autotune(b, days, chosen);
 }
 
 pt_status pt_batch_get_stage_ms(pt_batch *b, float ms[16], int days[2])

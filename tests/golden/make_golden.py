@@ -169,8 +169,11 @@ def main():
         raise SystemExit("the reference tree is needed to generate golden fixtures")
     if "--headline" in sys.argv:
         # about 40 minutes on one host core: the reference kernels run one thread
-        with open(os.path.join(HERE, "headline_50M_100d.json"), "w") as fh:
-            json.dump(headline_digest(*HEADLINE), fh)
+        g = headline_digest(*HEADLINE)
+        path = os.path.join(HERE, "headline_50M_100d.json")
+        with open(path + ".tmp", "w") as fh:
+            json.dump(g, fh)
+        os.replace(path + ".tmp", path)
         return
     with open(os.path.join(HERE, "rng.json"), "w") as fh:
         json.dump(rng_vectors(), fh)
