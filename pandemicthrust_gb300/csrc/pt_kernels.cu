@@ -1855,7 +1855,8 @@ __global__ void __launch_bounds__(256) k_infect_coop(InfectArgs a, int day)
             const int desired = prec_desired(rec.w);
             // the adult's errand profile from the schedule block on lane 6 (:3697-3702)
             const int pv = (j == 6) ? (int)(((lme & 1) ? (blk[2] ^ blk[3]) : (blk[0] ^ blk[1])) % 3u) : 0;
-            const int prof = adult ? __shfl_sync(kFull, pv, gl + 6) : 3;
+            const int pv6 = __shfl_sync(kFull, pv, gl + 6);   // every lane takes part in the shuffle
+            const int prof = adult ? pv6 : 3;
             if (j < 3) {
                 kv = select_victim(me, hoff, hcnt, wc, true, nullptr, victim);
             } else if (j < 3 + desired) {

@@ -199,7 +199,8 @@ def simulate(scenarios, replicates=1, persons=100_000, seed_base=1000, max_perso
 
     Returns a dict of arrays indexed [scenario, replicate, ...]: ``daily`` (DAYS x 2
     infected per day and strain, zero after the epidemic ends), ``attack`` (2, the
-    fraction ever infected), ``rn`` (GENERATIONS x 2), ``persons``.  Replicate r of
+    fraction ever infected), ``rn`` (GENERATIONS x 2), ``persons``, ``days`` (days
+    simulated, the statistics rows of the run).  Replicate r of
     scenario i uses core seed seed_base + i * replicates + r.
     """
     n, R = len(scenarios), int(replicates)
@@ -207,6 +208,7 @@ def simulate(scenarios, replicates=1, persons=100_000, seed_base=1000, max_perso
     attack = np.zeros((n, R, 2), np.float64)
     rn = np.zeros((n, R, GENERATIONS, 2), np.float64)
     npers = np.zeros((n, R), np.int64)
+    ndays = np.zeros((n, R), np.int64)
     jobs = [(i, r) for i in range(n) for r in range(R)]
     per_batch = max(1, min(4096, int(max_persons_per_batch // max(persons, 1))))
     for c0 in range(0, len(jobs), per_batch):
@@ -227,6 +229,7 @@ def simulate(scenarios, replicates=1, persons=100_000, seed_base=1000, max_perso
             N = b.info(k)["number_people"]
             npers[i, r] = N
             d = len(counts)
+            ndays[i, r] = d
             daily[i, r, :d, 0] = counts[:, 2:8].sum(axis=1)
             daily[i, r, :d, 1] = counts[:, 10:16].sum(axis=1)
             for s_, g in enumerate((gp[k], gs[k])):
@@ -235,7 +238,7 @@ def simulate(scenarios, replicates=1, persons=100_000, seed_base=1000, max_perso
                 nxt = g[1:GENERATIONS + 1].astype(np.float64)
                 rn[i, r, :, s_] = np.where(size > 0, nxt / np.maximum(size, 1), 0.0)
         b.close()
-    return {"daily": daily, "attack": attack, "rn": rn, "persons": npers}
+    return {"daily": daily, "attack": attack, "rn": rn, "persons": npers, "days": ndays}
 
 
 def targets(sim):
@@ -491,12 +494,110 @@ def evaluate(surrogate, scenarios, replicates, seed_base):
             "simulate_s": t_sim, "predict_s": t_pred}
 
 
+# ------------------------------------------------------------------ intervention search
+# Scenarios of the search: the pandemic and seasonal strains at R 1.5 / 1.2 with fixed
+# seeding, and the four interventions drawn from their ranges, school closure capped
+# by the closure-days budget.
+SEARCH_R = (1.5, 1.2)
+SEARCH_SEEDS_PER_MILLION = 20
+
+
+def search_scenarios(n, rng, budget_days):
+    """n intervention scenarios for the search: R fixed at SEARCH_R, seeds fixed (per
+    million persons; the surrogate takes them in its own population's numbers),
+    closure start uniform in its range, closure length uniform in [0, budget_days],
+    absenteeism and vaccination uniform in their ranges."""
+    lo, hi = RANGES["closure_start"]
+    out = []
+    for _ in range(n):
+        out.append({
+            "r_pandemic": SEARCH_R[0], "r_seasonal": SEARCH_R[1], "seeds": SEARCH_SEEDS_PER_MILLION,
+            "closure_start": int(rng.integers(lo, hi + 1)),
+            "closure_days": int(rng.integers(0, budget_days + 1)),
+            "absenteeism": float(rng.uniform(*RANGES["absenteeism"])),
+            "vaccination": float(rng.uniform(*RANGES["vaccination"])),
+        })
+    return out
+
+
+def scaled(scenario, persons, model_persons):
+    """The scenario for a population of `persons`: seed infections scale with the
+    population (same infected fraction at the start), everything else is kept."""
+    s = dict(scenario)
+    s["seeds"] = max(1, int(round(scenario["seeds"] * persons / model_persons)))
+    return s
+
+
+def transfer(pred, persons, model_persons):
+    """Predictions made at the model's population, carried to `persons` in fractions:
+    the network's population and the target's have the same structure per person
+    (households, schools, workplaces and errand locations all scale with persons), so
+    daily infected and peak height scale by persons / model_persons and attack rate
+    and peak day are kept."""
+    f = persons / float(model_persons)
+    out = dict(pred)
+    out["daily"] = pred["daily"] * f
+    out["peak"] = pred["peak"] * f
+    return out
+
+
+def search(surrogate, persons=50_000_000, candidates=100_000, budget_days=28, top_fraction=0.01, judge_top=None,
+           replicates=32, seed=2026, seed_base=300_000_000, max_persons_per_batch=700_000_000):
+    """Surrogate-screened intervention search.
+
+    Scores `candidates` random intervention scenarios with the surrogate (minimal
+    attack rate, both strains summed, under the closure-days budget), keeps the top
+    `top_fraction`, and re-simulates the best `judge_top` of those (default: all of
+    them) with `replicates` runs each at `persons` on the batched simulator, which
+    judges the surrogate (peak height and attack rate errors against the replicate
+    mean) and makes the final choice (the fallback: the simulator's best, not the
+    surrogate's, is returned).  Returns a dict of the timings, errors and choices."""
+    rng = np.random.default_rng(seed)
+    scen = search_scenarios(candidates, rng, budget_days)
+    X = features(scen)
+    surrogate.raw_features(X[:min(len(X), 4096)])   # warm-up
+    t0 = time.time()
+    Y = surrogate.raw_features(X)
+    t_score = time.time() - t0
+    pred = transfer(decode(Y, surrogate.persons), persons, surrogate.persons)
+    score = pred["attack"].sum(axis=1)
+    order = np.argsort(score, kind="stable")
+    top = order[:max(1, int(round(candidates * top_fraction)))]
+    judged = top if judge_top is None else top[:max(1, int(judge_top))]
+    big = [scaled(scen[i], persons, surrogate.persons) for i in judged]
+    t0 = time.time()
+    sim = simulate(big, replicates, persons, seed_base=seed_base, max_persons_per_batch=max_persons_per_batch)
+    t_sim = time.time() - t0
+    truth = truth_summary(sim)
+    sub = {k: np.asarray(v)[judged] for k, v in pred.items()}
+    pk, at = relative_errors(predicted_summary(sub), truth)
+    person_days = float((sim["persons"] * sim["days"]).sum())
+    abm_score = truth["attack"].sum(axis=1)
+    best_abm = int(np.argmin(abm_score))
+    return {
+        "persons": int(sim["persons"].mean()), "candidates": candidates, "budget_closure_days": budget_days,
+        "top": int(len(top)), "judged": int(len(judged)), "replicates": replicates,
+        "surrogate_scenarios_per_s": candidates / t_score, "surrogate_seconds": t_score,
+        "abm_seconds": t_sim, "abm_runs": int(len(judged) * replicates),
+        "abm_person_days_per_s": person_days / t_sim,
+        "error": {"peak_height_median": float(np.median(pk)), "peak_height_mean": float(np.mean(pk)),
+                  "attack_rate_median": float(np.median(at)), "attack_rate_mean": float(np.mean(at)),
+                  "pairs": int(len(pk)), "min_attack": 0.01},
+        "surrogate_choice": dict(scen[int(judged[0])], predicted_attack=[float(x) for x in pred["attack"][judged[0]]],
+                                 simulated_attack=[float(x) for x in truth["attack"][0]]),
+        "abm_choice": dict(scen[int(judged[best_abm])], simulated_attack=[float(x) for x in truth["attack"][best_abm]]),
+        "seeds_at_persons": big[0]["seeds"],
+    }
+
+
 def main(argv=None):
-    """python -m pandemicthrust_gb300.surrogate build|evaluate ...
+    """python -m pandemicthrust_gb300.surrogate build|evaluate|search ...
 
     build: samples scenarios, simulates each once on the batched simulator, trains
     an ensemble and saves it.  evaluate: scores a saved surrogate against fresh
-    simulations (mean of replicates)."""
+    simulations (mean of replicates).  search: the surrogate-screened intervention
+    search (``search``), by default 100,000 candidates at 50,000,000 persons with the
+    top 1% judged by 32 simulator replicates each."""
     import argparse
     ap = argparse.ArgumentParser(prog="python -m pandemicthrust_gb300.surrogate")
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -519,6 +620,15 @@ def main(argv=None):
     e.add_argument("--replicates", type=int, default=32)
     e.add_argument("--seed", type=int, default=99)
     e.add_argument("--seed-base", type=int, default=70_000_000)
+    q = sub.add_parser("search")
+    q.add_argument("--model", default=SHIPPED_MODEL)
+    q.add_argument("--persons", type=int, default=50_000_000)
+    q.add_argument("--candidates", type=int, default=100_000)
+    q.add_argument("--budget-days", type=int, default=28, help="closure-days budget")
+    q.add_argument("--top-fraction", type=float, default=0.01)
+    q.add_argument("--judge-top", type=int, default=None, help="re-simulate only the best N of the top fraction")
+    q.add_argument("--replicates", type=int, default=32)
+    q.add_argument("--seed", type=int, default=2026)
     a = ap.parse_args(argv)
     if a.cmd == "build":
         scen = sample_scenarios(a.train, np.random.default_rng(a.seed))
@@ -537,6 +647,11 @@ def main(argv=None):
         s.save(a.out, **info)
         s.close()
         print(json.dumps(info))
+    elif a.cmd == "search":
+        s = Surrogate.load(a.model, max_batch=65536)
+        r = search(s, a.persons, a.candidates, a.budget_days, a.top_fraction, a.judge_top, a.replicates, a.seed)
+        s.close()
+        print(json.dumps(r))
     else:
         s = Surrogate.load(a.model)
         scen = sample_scenarios(a.test, np.random.default_rng(a.seed))

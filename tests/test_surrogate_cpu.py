@@ -125,3 +125,22 @@ def test_nearest_neighbour_matches_brute_force():
     got = sg.nearest_neighbour(T, Y, X)[:, 0].astype(int)
     # ties aside (none in random data), the same training row
     np.testing.assert_array_equal(got, want)
+
+
+def test_search_scenarios_respect_the_budget_and_fixed_strains():
+    scen = sg.search_scenarios(2000, np.random.default_rng(3), budget_days=21)
+    assert all(s["closure_days"] <= 21 and s["r_pandemic"] == 1.5 and s["r_seasonal"] == 1.2 for s in scen)
+    assert max(s["closure_days"] for s in scen) == 21 and min(s["closure_days"] for s in scen) == 0
+    assert sg.in_range(scen).all()   # every candidate is inside the network's training ranges
+
+
+def test_transfer_to_a_larger_population_keeps_fractions():
+    pred = {"daily": np.ones((2, sg.DAYS, 2)) * 10.0, "peak": np.array([[5.0, 6.0], [7.0, 8.0]]),
+            "attack": np.array([[0.1, 0.2], [0.3, 0.4]]), "peak_day": np.array([[30.0, 40.0], [50.0, 60.0]])}
+    out = sg.transfer(pred, 50_000_000, 1_000_000)
+    np.testing.assert_array_equal(out["peak"], pred["peak"] * 50)
+    np.testing.assert_array_equal(out["daily"], pred["daily"] * 50)
+    np.testing.assert_array_equal(out["attack"], pred["attack"])
+    np.testing.assert_array_equal(out["peak_day"], pred["peak_day"])
+    s = sg.scaled({"seeds": 20, "closure_days": 3}, 50_000_000, 1_000_000)
+    assert s["seeds"] == 1000 and s["closure_days"] == 3
