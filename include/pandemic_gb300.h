@@ -189,6 +189,10 @@ typedef struct pt_tuning {
     int infect_coop;            /* 0: one thread per infector; 1: eight lanes per infector */
     int infect_blocks_per_sm;   /* infection grid, 256-thread blocks per SM: 1..32 */
     int radix_blocks_per_sm;    /* persistent blocks of a day's radix pass per SM: 1..3 */
+    int sched_tf;               /* the schedule kernel's Threefry arithmetic (same results):
+                                   0 integer adds and funnel shifts; 1 the 64-bit adds as
+                                   multiply-adds with carry; 2 also the rotations as wide
+                                   multiplies (moves work from the ALU to the FMA pipe) */
 } pt_tuning;
 
 /* Sets / reads the launch shapes of sim (allowed before or after pt_setup). */
@@ -276,6 +280,9 @@ pt_status pt_mlp_predict(pt_mlp *mlp, const float *x, int n, float *y);
 /* the mean output of `count` networks of one shape on n rows (an ensemble): all run
  * on the first network's stream, the mean is formed on the device and copied once */
 pt_status pt_mlp_predict_ensemble(pt_mlp *const *members, int count, const float *x, int n, float *y);
+/* The same with x (n x widths[0]) and y (n x widths[layers]) in device memory: no
+ * copies and no synchronisation; the work is queued on the first network's stream. */
+pt_status pt_mlp_predict_ensemble_device(pt_mlp *const *members, int count, const float *x, int n, float *y);
 void pt_mlp_destroy(pt_mlp *mlp);
 const char *pt_mlp_last_error(const pt_mlp *mlp);
 

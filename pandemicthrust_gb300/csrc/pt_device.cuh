@@ -106,6 +106,77 @@ __device__ __forceinline__ void tf2x64(const TfKey &k, uint64_t ctr, uint32_t w[
     w[0] = x0.lo; w[1] = x0.hi; w[2] = x1.lo; w[3] = x1.hi;
 }
 
+// The same Threefry-2x64-20 with part of its integer work moved from the ALU pipe
+// (IADD3 / SHF / LOP3) to the multiply-add pipe.  `m` holds run-time constants (kernel
+// parameters, so the compiler cannot fold the multiplies back into adds and shifts):
+// m.one = 1 and m.pow[i] = 2^r for the rotation amounts r below 32.
+//   MODE 1: every 64-bit add is a multiply-add with carry, x * 1 + y.
+//   MODE 2: also every rotation: x * 2^r as a 32 x 32 -> 64 multiply gives both
+//           halves of x shifted by r; two of them and an OR rotate a 64-bit word, and
+//           the OR folds into the round's XOR.
+// Bit-identical to tf2x64 (integer arithmetic, exact in every form).
+struct TfMul {
+    uint32_t one;
+    uint32_t pow[6];   // 2^16, 2^10 (rotation 42 = swap + 10), 2^12, 2^31, 2^24, 2^21
+};
+
+__device__ __forceinline__ u64h add64m(u64h a, u64h b, uint32_t one)
+{
+    u64h r;
+    asm("mad.lo.cc.u32 %0, %2, %6, %4;\n\tmadc.lo.u32 %1, %3, %6, %5;"
+        : "=r"(r.lo), "=r"(r.hi) : "r"(a.lo), "r"(a.hi), "r"(b.lo), "r"(b.hi), "r"(one));
+    return r;
+}
+
+// rotate left by r in (0, 32) with p = 2^r: the 64-bit products hold (x << r) in the
+// low word and (x >> (32 - r)) in the high word
+__device__ __forceinline__ u64h rotl64m(u64h x, uint32_t p)
+{
+    const unsigned long long t = (unsigned long long)x.lo * p, u = (unsigned long long)x.hi * p;
+    return {(uint32_t)t | (uint32_t)(u >> 32), (uint32_t)u | (uint32_t)(t >> 32)};
+}
+
+template <int MODE, int R, int PI>
+__device__ __forceinline__ void mix64m(u64h &x0, u64h &x1, const TfMul &m)
+{
+    x0 = MODE >= 1 ? add64m(x0, x1, m.one) : add64(x0, x1);
+    if constexpr (MODE >= 2 && R != 32) {
+        const u64h s = R > 32 ? u64h{x1.hi, x1.lo} : x1;
+        x1 = rotl64m(s, m.pow[PI]);
+    } else {
+        x1 = rotl64<R>(x1);
+    }
+    x1.lo ^= x0.lo;
+    x1.hi ^= x0.hi;
+}
+
+template <int MODE>
+__device__ __forceinline__ void tf2x64m(const TfKey &k, uint64_t ctr, uint32_t w[4], const TfMul &m)
+{
+    if constexpr (MODE == 0) {
+        tf2x64(k, ctr, w);
+    } else {
+        const u64h c = mk(ctr);
+        u64h x0 = add64m(c, k.k0, m.one);
+        u64h x1 = add64m(c, k.k1, m.one);
+        const u64h ks[3] = {k.k0, k.k1, k.k2};
+#pragma unroll
+        for (int blk = 0; blk < 5; blk++) {
+            if ((blk & 1) == 0) {
+                mix64m<MODE, 16, 0>(x0, x1, m); mix64m<MODE, 42, 1>(x0, x1, m);
+                mix64m<MODE, 12, 2>(x0, x1, m); mix64m<MODE, 31, 3>(x0, x1, m);
+            } else {
+                mix64m<MODE, 16, 0>(x0, x1, m); mix64m<MODE, 32, 0>(x0, x1, m);
+                mix64m<MODE, 24, 4>(x0, x1, m); mix64m<MODE, 21, 5>(x0, x1, m);
+            }
+            const int s = blk + 1;
+            x0 = add64m(x0, ks[s % 3], m.one);
+            x1 = add64m(x1, add64(ks[(s + 1) % 3], u64h{(uint32_t)s, 0u}), m.one);
+        }
+        w[0] = x0.lo; w[1] = x0.hi; w[2] = x1.lo; w[3] = x1.hi;
+    }
+}
+
 template <int R>
 __device__ __forceinline__ void mix32(uint32_t &x0, uint32_t &x1)
 {
@@ -223,12 +294,18 @@ __device__ __forceinline__ int fish_weekend_dest(const SimConst &c, uint32_t r)
 // weekend destinations all lie in [lo, L) (lo = first location of type 9), so the
 // bucket index used here is the order-preserving compact form hour * R + dest - lo,
 // R = L - lo.
+template <int MODE = 0>
 __device__ __forceinline__ void weekend_errands(const SimConst &c, const TfKey &k, uint64_t ctr, int lo, int R,
-                                                int out[3])
+                                                int out[3], const TfMul *m = nullptr)
 {
     uint32_t w[8];
-    tf2x64(k, ctr, w);
-    tf2x64(k, ctr + 1, w + 4);
+    if constexpr (MODE == 0) {
+        tf2x64(k, ctr, w);
+        tf2x64(k, ctr + 1, w + 4);
+    } else {
+        tf2x64m<MODE>(k, ctr, w, *m);
+        tf2x64m<MODE>(k, ctr + 1, w + 4, *m);
+    }
     int h1 = (int)(w[0] % 10u);
     int h2 = (int)(w[1] % 10u);
     if (h2 == h1) h2 = (h2 + 1) % 10;

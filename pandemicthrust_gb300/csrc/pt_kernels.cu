@@ -1145,12 +1145,12 @@ __global__ void k_mark_buckets(const InstConst *ic, const InstState *is, const u
 // instance's constants are staged in shared memory.
 constexpr int kSchedThreads = 256, kSchedTile = kPersonTile, kSchedWarpPersons = 512;
 
-template <bool WEEKEND>
+template <bool WEEKEND, int TF>
 __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic, InstState *is,
                                                          const int32_t *tile_inst, int K, const uint8_t *age,
                                                          const uint32_t *mark, int32_t *keys, int *digit_hist,
                                                          int passes, uint32_t *ckeys, uint32_t *cvals, Scalars *sc,
-                                                         LookBack lb, int day)
+                                                         LookBack lb, int day, TfMul tm)
 {
     if (*(volatile int *)&sc->done) return;
     __shared__ int s_dh[kMaxRadixPasses][256];   // digit histograms of the marked entries
@@ -1196,7 +1196,7 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
             bool mk[3] = {false, false, false};
             if (i < valid) {
                 int d[3];
-                weekend_errands(c, key, E0 + 2ull * (unsigned long long)(tbase + i), lo, R, d);
+                weekend_errands<TF>(c, key, E0 + 2ull * (unsigned long long)(tbase + i), lo, R, d, &tm);
 #pragma unroll
                 for (int k = 0; k < 3; k++) {
                     kb[k] = (uint32_t)(bb + d[k]);
@@ -1219,7 +1219,7 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
             bool mk[4] = {false, false, false, false};
             if (i < valid) {
                 uint32_t w[4];
-                tf2x64(key, E0 + (uint64_t)((tbase + i) / 2), w);
+                tf2x64m<TF>(key, E0 + (uint64_t)((tbase + i) / 2), w, tm);
 #pragma unroll
                 for (int k = 0; k < 2; k++) {
                     if (i + k < valid) {
@@ -1318,6 +1318,16 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
     lookback_end(lb);
 }
 
+// The run-time constants of tf2x64m: 1 and the powers of two of the rotations.
+static TfMul tf_multipliers()
+{
+    TfMul m;
+    m.one = 1u;
+    const int r[6] = {16, 10, 12, 31, 24, 21};
+    for (int i = 0; i < 6; i++) m.pow[i] = 1u << r[i];
+    return m;
+}
+
 int day_buckets(const SimConst &c, bool weekend)
 {
     return weekend ? 10 * (c.L - c.type_offset[9]) : 2 * (c.L - c.type_offset[8]);
@@ -1339,12 +1349,21 @@ cudaError_t launch_schedule(const DevArrays &d, bool weekend, int day, bool full
     const int blocks = d.P / kSchedTile;
     const LookBack lb = make_lb(d);
     const int passes = radix_passes(d.bucket_max[weekend ? 1 : 0]);
-    if (weekend)
-        k_sched<true><<<blocks, kSchedThreads, 0, s>>>(
-            d.ic, d.is, d.tile_inst, d.K, d.age, d.mark, d.keys, d.digit_hist, passes, d.rk1, d.rv1, d.sc, lb, day);
-    else
-        k_sched<false><<<blocks, kSchedThreads, 0, s>>>(
-            d.ic, d.is, d.tile_inst, d.K, d.age, d.mark, d.keys, d.digit_hist, passes, d.rk1, d.rv1, d.sc, lb, day);
+    const TfMul tm = tf_multipliers();
+#define PT_SCHED(W, T)                                                                                              \
+    k_sched<W, T><<<blocks, kSchedThreads, 0, s>>>(d.ic, d.is, d.tile_inst, d.K, d.age, d.mark, d.keys, d.digit_hist, \
+                                                    passes, d.rk1, d.rv1, d.sc, lb, day, tm)
+    const int tf = d.tune.sched_tf;
+    if (weekend) {
+        if (tf == 2) PT_SCHED(true, 2);
+        else if (tf == 1) PT_SCHED(true, 1);
+        else PT_SCHED(true, 0);
+    } else {
+        if (tf == 2) PT_SCHED(false, 2);
+        else if (tf == 1) PT_SCHED(false, 1);
+        else PT_SCHED(false, 0);
+    }
+#undef PT_SCHED
     count_launch();
     return cudaGetLastError();
 }

@@ -88,6 +88,8 @@ struct Tuning {
     int infect_blocks_per_sm = 8;   // infection grid: 256-thread blocks per SM (twice as
                                     // many 128-thread blocks for the thread-per-infector kernels)
     int radix_blocks_per_sm = 3;    // persistent blocks of a day's radix pass per SM (1..3)
+    int sched_tf = 0;               // schedule kernel's Threefry arithmetic: 0 ALU adds and
+                                    // shifts, 1 multiply-add adds, 2 also multiply rotations
 };
 
 // Device pointers of a batch of simulations (one simulation is a batch of one).

@@ -609,6 +609,45 @@ pt_status pt_mlp_predict_ensemble(pt_mlp *const *members, int count, const float
     return PT_OK;
 }
 
+pt_status pt_mlp_predict_ensemble_device(pt_mlp *const *members, int count, const float *X, int n, float *Y)
+{
+    if (!members || count < 1 || !X || !Y || n < 0) return PT_ERR_ARG;
+    pt_mlp *m = members[0];
+    if (!m) return PT_ERR_ARG;
+    int chunk = m->max_batch;
+    for (int j = 0; j < count; j++) {
+        pt_mlp *q = members[j];
+        if (!q) return PT_ERR_ARG;
+        if (q->L != m->L) return mfail(m, PT_ERR_ARG, "ensemble members differ in depth");
+        for (int l = 0; l <= m->L; l++)
+            if (q->width[l] != m->width[l]) return mfail(m, PT_ERR_ARG, "ensemble members differ in widths");
+        chunk = std::min(chunk, q->max_batch);
+    }
+    const int din = m->width[0], dout = m->width[m->L];
+    const cudaStream_t s = m->stream;
+    for (int j = 1; j < count; j++)
+        if (members[j]->stream != s) MCK(cudaStreamSynchronize(members[j]->stream), "ensemble member stream");
+    for (int s0 = 0; s0 < n; s0 += chunk) {
+        const int B = std::min(chunk, n - s0);
+        for (int j = 0; j < count; j++) {
+            pt_mlp *q = members[j];
+            const cudaStream_t own = q->stream;
+            q->stream = s;
+            k_gather<<<B, 128, 0, s>>>(X + (size_t)s0 * din, nullptr, nullptr, B, din, dout, q->H[0], nullptr);
+            cudaError_t e = forward(q, B);
+            if (e == cudaSuccess) {
+                const long long total = (long long)B * dout;
+                k_accumulate<<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, s>>>(
+                    Y + (size_t)s0 * dout, q->Z[q->L - 1], total, 1.0f / (float)count, j == 0);
+                e = cudaGetLastError();
+            }
+            q->stream = own;
+            MCK(e, "ensemble predict (device)");
+        }
+    }
+    return PT_OK;
+}
+
 void pt_mlp_destroy(pt_mlp *m)
 {
     if (!m) return;

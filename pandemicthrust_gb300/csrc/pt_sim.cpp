@@ -837,20 +837,23 @@ static pt_tuning to_public(const ptk::Tuning &t)
     o.infect_coop = t.infect_coop;
     o.infect_blocks_per_sm = t.infect_blocks_per_sm;
     o.radix_blocks_per_sm = t.radix_blocks_per_sm;
+    o.sched_tf = t.sched_tf;
     return o;
 }
 
 static pt_status engine_set_tuning(Engine *s, const pt_tuning *t)
 {
     if (!t || (t->infect_coop != 0 && t->infect_coop != 1) || t->infect_blocks_per_sm < 1 ||
-        t->infect_blocks_per_sm > 32 || t->radix_blocks_per_sm < 1 || t->radix_blocks_per_sm > 3)
+        t->infect_blocks_per_sm > 32 || t->radix_blocks_per_sm < 1 || t->radix_blocks_per_sm > 3 ||
+        t->sched_tf < 0 || t->sched_tf > 2)
         return fail(s, PT_ERR_ARG, "launch shape outside its range");
     ptk::Tuning n;
     n.infect_coop = t->infect_coop;
     n.infect_blocks_per_sm = t->infect_blocks_per_sm;
     n.radix_blocks_per_sm = t->radix_blocks_per_sm;
+    n.sched_tf = t->sched_tf;
     if (n.infect_coop != s->d.tune.infect_coop || n.infect_blocks_per_sm != s->d.tune.infect_blocks_per_sm ||
-        n.radix_blocks_per_sm != s->d.tune.radix_blocks_per_sm) {
+        n.radix_blocks_per_sm != s->d.tune.radix_blocks_per_sm || n.sched_tf != s->d.tune.sched_tf) {
         // the captured day loop holds the old launch shapes
         if (s->stream) cudaStreamSynchronize(s->stream);
         if (s->run_graph) cudaGraphExecDestroy(s->run_graph);
@@ -870,9 +873,9 @@ static std::vector<long long> tune_key(const Engine *s)
             s->max_days, ptk::sm_count()};
 }
 
-// The tuner.  The infection stage and the radix stage are timed separately (per-stage
+// The tuner.  The infection, radix and schedule stages are timed separately (per-stage
 // CUDA events around every day), so one run measures one candidate of each: run i
-// uses infection candidate i and radix candidate i % 3.
+// uses infection candidate i, radix candidate i % 3 and Threefry form (i + 1) % 3.
 static pt_status engine_autotune(Engine *s, int days, pt_tuning *chosen)
 {
     if (!s->setup_done) return fail(s, PT_ERR_STATE, "autotune before setup");
@@ -892,8 +895,9 @@ static pt_status engine_autotune(Engine *s, int days, pt_tuning *chosen)
     // warp-cooperative kernel: 6 resident 256-thread blocks per SM at 40 registers
     const Cand infect[] = {{0, 8}, {0, 4}, {1, 6}, {1, 12}, {1, 3}, {0, 16}};
     const int radix[] = {3, 2, 1};
+    const int tfs[] = {0, 1, 2};
     const int runs = (int)(sizeof(infect) / sizeof(infect[0]));
-    float best_inf = 1e30f, best_rad[3] = {1e30f, 1e30f, 1e30f};
+    float best_inf = 1e30f, best_rad[3] = {1e30f, 1e30f, 1e30f}, best_tf[3] = {1e30f, 1e30f, 1e30f};
     int best_i = 0;
     const int saved_max = s->max_days;
     const int trial = days > 0 ? std::min(days, saved_max) : saved_max;
@@ -902,6 +906,7 @@ static pt_status engine_autotune(Engine *s, int days, pt_tuning *chosen)
         t.infect_coop = infect[i].coop;
         t.infect_blocks_per_sm = infect[i].bps;
         t.radix_blocks_per_sm = radix[i % 3];
+        t.sched_tf = tfs[(i + 1) % 3];
         pt_status st = engine_set_tuning(s, &t);
         if (st == PT_OK) st = engine_reset(s);
         if (st == PT_OK) st = engine_set_timing(s, 1);
@@ -914,19 +919,24 @@ static pt_status engine_autotune(Engine *s, int days, pt_tuning *chosen)
         engine_stage_ms(s, ms, nullptr);
         const float inf = ms[kStInfect] + ms[8 + kStInfect];
         const float rad = ms[kStRadix] + ms[8 + kStRadix];
+        const float sch = ms[kStSchedule] + ms[8 + kStSchedule];
+        best_tf[(i + 1) % 3] = std::min(best_tf[(i + 1) % 3], sch);
         if (inf < best_inf) {
             best_inf = inf;
             best_i = i;
         }
         best_rad[i % 3] = std::min(best_rad[i % 3], rad);
     }
-    int rbest = 0;
-    for (int r = 1; r < 3; r++)
+    int rbest = 0, tbest = 0;
+    for (int r = 1; r < 3; r++) {
         if (best_rad[r] < best_rad[rbest]) rbest = r;
+        if (best_tf[r] < best_tf[tbest]) tbest = r;
+    }
     pt_tuning t;
     t.infect_coop = infect[best_i].coop;
     t.infect_blocks_per_sm = infect[best_i].bps;
     t.radix_blocks_per_sm = radix[rbest];
+    t.sched_tf = tfs[tbest];
     pt_status st = engine_set_timing(s, 0);
     if (st == PT_OK) st = engine_set_tuning(s, &t);
     if (st == PT_OK) st = engine_reset(s);

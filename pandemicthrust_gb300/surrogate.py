@@ -65,6 +65,7 @@ class MLP:
         lib.pt_mlp_gradients.argtypes = [vp, fp, fp, ctypes.c_int, fp, fp]
         lib.pt_mlp_predict.argtypes = [vp, fp, ctypes.c_int, fp]
         lib.pt_mlp_predict_ensemble.argtypes = [ctypes.POINTER(vp), ctypes.c_int, fp, ctypes.c_int, fp]
+        lib.pt_mlp_predict_ensemble_device.argtypes = [ctypes.POINTER(vp), ctypes.c_int, vp, ctypes.c_int, vp]
         lib.pt_mlp_destroy.argtypes = [vp]
         lib.pt_mlp_last_error.argtypes = [vp]
         lib.pt_mlp_last_error.restype = ctypes.c_char_p
@@ -381,6 +382,14 @@ class Surrogate:
         members = (ctypes.c_void_p * len(self.nets))(*[net.h.value for net in self.nets])
         net0._check(net0.lib.pt_mlp_predict_ensemble(members, len(self.nets), MLP._f(X), len(X), MLP._f(Y)))
         return Y
+
+    def raw_device(self, x_ptr, n, y_ptr):
+        """The ensemble mean on device buffers (float32, n x inputs -> n x outputs),
+        queued on the first network's stream without copies or synchronisation."""
+        net0 = self.nets[0]
+        members = (ctypes.c_void_p * len(self.nets))(*[net.h.value for net in self.nets])
+        net0._check(net0.lib.pt_mlp_predict_ensemble_device(members, len(self.nets), ctypes.c_void_p(x_ptr), int(n),
+                                                             ctypes.c_void_p(y_ptr)))
 
     def predict(self, scenarios, fallback_replicates=4, seed_base=900_000):
         """Decoded predictions; scenarios outside the training ranges are simulated
