@@ -325,6 +325,7 @@ constexpr int kRadixTile = kRadixThreads * kRadixItems;
 static_assert(kRadixTile == kRadixTileEntries, "the host sizes the radix look-back words by kRadixTileEntries");
 
 enum RadixMode { kRadixFirst = 0, kRadixMiddle = 1, kRadixLast = 2, kRadixOnly = 3 };
+constexpr uint32_t kDropped = 0xFFFFFFFFu;   // value of an entry a pass leaves out (no person id is this)
 
 // Person id of schedule entry i: the setup table is the identity, weekday entries
 // are hour-major (i < N hour 0, else hour 1), weekend entries person-major (3 per person).
@@ -384,7 +385,9 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
 {
     if (skip && *(volatile const int *)skip) return;
     __shared__ int s_tile;
-    __shared__ int s_seg[4];      // segment, tile within it, entry base, entry count
+    // segment, tile within it, entry base, entry count; for a dense segment of a day's
+    // first pass: 1, the instance's persons, first person and first bucket
+    __shared__ int s_seg[8];
     __shared__ unsigned s_epoch;
     __shared__ int s_hist[kRadixWarps][256];
     __shared__ int s_base[256];   // global position of the tile's first entry of each digit
@@ -392,9 +395,12 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
     __shared__ uint32_t s_key[kRadixTile];
     __shared__ uint32_t s_val[kRadixTile];
     const int shift = 8 * pass;
+    // first pass of a day's sort (explicit values: the setup sorts' implicit modes never are)
+    const bool day0 = (MODE == kRadixMiddle || MODE == kRadixLast) && sg.day_keys != nullptr && pass == 0;
+    const int *tprefix = day0 ? sg.tile_prefix0 : sg.tile_prefix;
     int E = 0, tiles;
     if (sg.tile_prefix) {
-        tiles = *(volatile const int *)&sg.tile_prefix[sg.segments];
+        tiles = *(volatile const int *)&tprefix[sg.segments];
     } else {
         E = count_dev ? *(volatile const int *)count_dev : E_arg;
         tiles = (E + kRadixTile - 1) / kRadixTile;
@@ -408,53 +414,82 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
     for (;;) {
         if (threadIdx.x == 0) {
             const int t = atomicAdd(&ctl[0], 1);
-            int k = 0, j = t, sbase = 0, scount = E;
+            int k = 0, j = t, sbase = 0, scount = E, dense = 0, nk = 0, pb = 0, bb = 0;
             if (sg.tile_prefix && t < tiles) {
-                // the segment owning tile t: the last k with tile_prefix[k] <= t
+                // the segment owning tile t: the last k with tprefix[k] <= t
                 int lo = 0, hi = sg.segments - 1;
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
-                    if (sg.tile_prefix[mid] <= t) lo = mid;
+                    if (tprefix[mid] <= t) lo = mid;
                     else hi = mid - 1;
                 }
                 k = lo;
-                j = t - sg.tile_prefix[k];
+                j = t - tprefix[k];
                 sbase = (int)sg.ic[k].kbase;
                 scount = sg.is[k].marked;
+                if (day0 && sg.is[k].dense) {
+                    dense = 1;
+                    nk = sg.ic[k].c.N;
+                    pb = sg.ic[k].pbase;
+                    bb = sg.ic[k].bbase[sg.weekend];
+                    scount = (sg.weekend ? 3 : 2) * nk;   // every schedule key of the instance
+                }
             }
             s_tile = t;
             s_seg[0] = k;
             s_seg[1] = j;
             s_seg[2] = sbase;
             s_seg[3] = scount;
+            s_seg[4] = dense;
+            s_seg[5] = nk;
+            s_seg[6] = pb;
+            s_seg[7] = bb;
         }
         __syncthreads();
         const int tile = s_tile;
         const unsigned epoch = s_epoch;
         if (tile >= tiles) break;
         const int seg = s_seg[0], stile = s_seg[1], sbase = s_seg[2], scount = s_seg[3];
+        const bool dense = s_seg[4] != 0;
         for (int i = threadIdx.x; i < kRadixWarps * 256; i += kRadixThreads) (&s_hist[0][0])[i] = 0;
         __syncthreads();
         const int base = stile * kRadixTile + warp * kRadixWarpItems + lane;  // index within the segment
         const bool full = (stile + 1) * kRadixTile <= scount;
         uint32_t key[kRadixItems], val[kRadixItems], info[kRadixItems];
+        if (dense) {
+            // the instance's schedule keys, persons implicit (weekday hour-major: entry
+            // i < N is person i's hour-0 key, i >= N person i - N's hour-1 key; weekend
+            // person-major, three per person), instance-local bucket keys; an entry of
+            // an unmarked bucket gets the value kDropped and is left out
+            const int nk = s_seg[5], pb = s_seg[6], bb = s_seg[7];
 #pragma unroll
-        for (int j = 0; j < kRadixItems; j++) {
-            const int i = base + 32 * j;
-            const bool in = full || i < scount;
-            key[j] = in ? keys_in[sbase + i] : 0u;
-            if (MODE == kRadixFirst || MODE == kRadixOnly) {
-                const uint32_t u = (uint32_t)i;
-                val[j] = person_mode == 0 ? u : (person_mode == 1 ? (u < (uint32_t)N ? u : u - (uint32_t)N) : u / 3u);
-            } else {
-                val[j] = in ? vals_in[sbase + i] : 0u;
+            for (int j = 0; j < kRadixItems; j++) {
+                const int i = base + 32 * j;
+                const bool in = full || i < scount;
+                const int kg = in ? sg.day_keys[sbase + i] : bb;
+                key[j] = (uint32_t)(kg - bb);
+                const bool marked = in && ((sg.mark[kg >> 5] >> (kg & 31)) & 1u);
+                val[j] = marked ? (uint32_t)(pb + (sg.weekend ? i / 3 : (i < nk ? i : i - nk))) : kDropped;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < kRadixItems; j++) {
+                const int i = base + 32 * j;
+                const bool in = full || i < scount;
+                key[j] = in ? keys_in[sbase + i] : 0u;
+                if (MODE == kRadixFirst || MODE == kRadixOnly) {
+                    const uint32_t u = (uint32_t)i;
+                    val[j] = person_mode == 0 ? u : (person_mode == 1 ? (u < (uint32_t)N ? u : u - (uint32_t)N) : u / 3u);
+                } else {
+                    val[j] = in ? vals_in[sbase + i] : 0u;
+                }
             }
         }
         // phase A: rank within the warp round, per-warp digit counts
 #pragma unroll
         for (int j = 0; j < kRadixItems; j++) {
             const int i = base + 32 * j;
-            bool ok = full || i < scount;
+            bool ok = (full || i < scount) && val[j] != kDropped;
             if ((MODE == kRadixFirst || MODE == kRadixOnly) && mark && ok)
                 ok = (mark[key[j] >> 5] >> (key[j] & 31u)) & 1u;
             const unsigned d = (key[j] >> shift) & 255u;
@@ -911,6 +946,7 @@ __global__ void __launch_bounds__(kSweepThreads, 8) k_sweep_count(const InstCons
 }
 
 constexpr int kSweepScanThreads = 1024;
+constexpr int kDenseInfected = 4;   // dense day: kDenseInfected x infected >= the instance's buckets
 
 __global__ void __launch_bounds__(kSweepScanThreads) k_sweep_scan(const InstConst *ic, InstState *is, int K,
                                                                   int32_t *tile_count, int tiles, Scalars *sc,
@@ -940,12 +976,18 @@ __global__ void __launch_bounds__(kSweepScanThreads) k_sweep_scan(const InstCons
         const int start = tile_count[ic[k].pbase / kSweepTile], end = tile_count[ic[k].pend / kSweepTile];
         s.start = start;
         s.list_end = end;
+        s.marked = 0;
+        s.dense = 0;
         if (!instance_running(ic[k], s, day)) {
             s.infected = 0;
             continue;
         }
         const int I = end - start;
         s.infected = I;
+        // Most of today's buckets will be read when the infected (each marks one or two
+        // buckets) number at least a quarter of the buckets: then the sort reads the
+        // schedule keys directly.  Either way the tables are the same.
+        s.dense = (long long)kDenseInfected * I >= (long long)ic[k].bcount[weekend ? 1 : 0] ? 1 : 0;
         s.infected_per_day[day] = I;
         s.day = day;
         s.days_run = day + 1;
@@ -1249,7 +1291,16 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
     for (int o = 16; o > 0; o >>= 1) wt += __shfl_xor_sync(0xffffffffu, wt, o);
     if (lane == 0) s_wtot[warp] = wt;
     __syncthreads();
-    if (warp == 0) {
+    // A dense instance (most of today's buckets are read): the sort's first pass reads
+    // the keys written above, so only the marked count is needed, not the entries.
+    const bool dense = is[inst].dense != 0;
+    if (dense) {
+        if (threadIdx.x == 0) {
+            int tot = 0;
+            for (int w = 0; w < kSchedThreads / 32; w++) tot += s_wtot[w];
+            if (tot) red_add(&is[inst].marked, tot);
+        }
+    } else if (warp == 0) {
         // the instance's entries form their own segment: its first tile starts the scan
         int tot = 0;
         for (int w = 0; w < kSchedThreads / 32; w++) tot += s_wtot[w];
@@ -1270,6 +1321,10 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
             const int v = s_dh[p][threadIdx.x];
             if (v) red_add(&h[p * 256 + threadIdx.x], v);
         }
+    }
+    if (dense) {
+        lookback_end(lb);
+        return;
     }
     ckeys += ic[inst].kbase;   // the instance's segment of the entry arrays
     cvals += ic[inst].kbase;
@@ -1368,10 +1423,12 @@ cudaError_t launch_schedule(const DevArrays &d, bool weekend, int day, bool full
     return cudaGetLastError();
 }
 
-// The day's radix sort starts from the marked entries the schedule appended to each
-// instance's segment of (rk1, rv1), in person order: one sorted segment per instance,
-// keys local to the instance, so the passes cover the largest instance's buckets
-// only.
+// The day's radix sort: one sorted segment per instance, keys local to the instance,
+// so the passes cover the largest instance's buckets only.  A segment's first pass
+// reads the marked entries the schedule appended to the instance's part of (rk1, rv1)
+// in person order, or, for an instance dense today, every schedule key (keeping the
+// marked ones).  Equal keys come from one hour, in person order, in both inputs, so
+// the sorted tables are the same.
 static RadixArgs day_radix_args(const DevArrays &d, bool weekend)
 {
     RadixArgs r;
@@ -1388,6 +1445,10 @@ static RadixArgs day_radix_args(const DevArrays &d, bool weekend)
     r.seg.ic = d.ic;
     r.seg.is = d.is;
     r.seg.segments = d.K;
+    r.seg.day_keys = d.keys;
+    r.seg.tile_prefix0 = d.tile_prefix0;
+    r.seg.mark = d.mark;
+    r.seg.weekend = weekend ? 1 : 0;
     r.status = d.radix_status;
     r.ctl = d.radix_ctl;
     r.error = &d.sc->error;
@@ -1401,8 +1462,9 @@ static RadixArgs day_radix_args(const DevArrays &d, bool weekend)
 // the schedule kernel accumulated (summing the stripes, clearing them).  Block 0
 // also numbers the segments' radix tiles (tile_prefix) and adds the day's
 // materialised entries to the running total.
-__global__ void k_day_digit_bases(int *digit_hist, int *digit_base, int passes, const InstState *is, int K,
-                                  int32_t *tile_prefix, Scalars *sc)
+__global__ void k_day_digit_bases(int *digit_hist, int *digit_base, int passes, const InstConst *ic,
+                                  const InstState *is, int K, int weekend, int32_t *tile_prefix,
+                                  int32_t *tile_prefix0, Scalars *sc)
 {
     if (*(volatile const int *)&sc->done) return;
     const int k = blockIdx.x;
@@ -1418,21 +1480,28 @@ __global__ void k_day_digit_bases(int *digit_hist, int *digit_base, int passes, 
         digit_base[((size_t)k * passes + p) * 256 + threadIdx.x] = excl;
     }
     if (k != 0) return;
-    int carry = 0;
+    int carry = 0, carry0 = 0;
     unsigned long long entries = 0;
     for (int b = 0; b < K; b += 256) {
         const int i = b + (int)threadIdx.x;
         const int m = i < K ? is[i].marked : 0;
+        // the first pass reads every key of a dense instance, the appended entries otherwise
+        const int m0 = (i < K && is[i].dense) ? (weekend ? 3 : 2) * ic[i].c.N : m;
         int total;
         const int excl = block_exclusive_scan<256, int>((m + kRadixTile - 1) / kRadixTile, total);
         if (i < K) tile_prefix[i] = carry + excl;
         carry += total;
+        int total0;
+        const int excl0 = block_exclusive_scan<256, int>((m0 + kRadixTile - 1) / kRadixTile, total0);
+        if (i < K) tile_prefix0[i] = carry0 + excl0;
+        carry0 += total0;
         int msum;
         block_exclusive_scan<256, int>(m, msum);
         entries += (unsigned long long)msum;
     }
     if (threadIdx.x == 0) {
         tile_prefix[K] = carry;
+        tile_prefix0[K] = carry0;
         sc->materialised_sum += entries;
     }
 }
@@ -1440,7 +1509,8 @@ __global__ void k_day_digit_bases(int *digit_hist, int *digit_base, int passes, 
 cudaError_t launch_bucket_scan(const DevArrays &d, bool weekend, cudaStream_t s)
 {
     const int P = radix_passes(d.bucket_max[weekend ? 1 : 0]);
-    k_day_digit_bases<<<d.K, 256, 0, s>>>(d.digit_hist, d.digit_base, P, d.is, d.K, d.tile_prefix, d.sc);
+    k_day_digit_bases<<<d.K, 256, 0, s>>>(d.digit_hist, d.digit_base, P, d.ic, d.is, d.K, weekend ? 1 : 0,
+                                          d.tile_prefix, d.tile_prefix0, d.sc);
     count_launch();
     return cudaGetLastError();
 }

@@ -62,6 +62,8 @@ struct InstState {
     int start;                          // their first position in the batch's infected list
     int list_end;                       // one past their last position
     int marked;                         // today's schedule entries in materialised buckets
+    int dense;                          // today's sort reads the schedule keys directly (most
+                                        // buckets are read) instead of entries the schedule appended
     int done;                           // set once a day counts zero infected
     int days_run;                       // statistics rows written
     int day;                            // last day run
@@ -115,6 +117,7 @@ struct DevArrays {
     int *digit_hist;          // K x kDigitStripes x 4 x 256 (the first 4 x 256 also serve the setup sorts)
     int *digit_base;          // K x 4 x 256
     int32_t *tile_prefix;     // K + 1: radix tiles of the instances' segments
+    int32_t *tile_prefix0;    // K + 1: the same for the first pass (a dense segment's input is all its keys)
     uint32_t *mark;           // bitmap over today's buckets: 1 = materialise
     int32_t *infected;        // P ascending infected ids
     int32_t *infected_inst;   // P: instance of each infected list position
@@ -179,6 +182,15 @@ struct RadixSegments {
     const InstConst *ic = nullptr;
     const InstState *is = nullptr;
     int segments = 0;
+    // The day's sort: in its first pass a segment whose instance is dense today reads
+    // its entries straight from the schedule keys (global bucket ids at
+    // day_keys[kbase ...], 2N weekday hour-major / 3N weekend person-major, persons
+    // implicit), keeping those of marked buckets; the other segments read the
+    // entries the schedule appended.  tile_prefix0 numbers the first pass's tiles.
+    const int32_t *day_keys = nullptr;
+    const int *tile_prefix0 = nullptr;
+    const uint32_t *mark = nullptr;
+    int weekend = 0;
 };
 
 // Stable LSD radix sort of E keys in [0, buckets) with implicit person values

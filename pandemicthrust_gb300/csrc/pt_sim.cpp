@@ -377,7 +377,7 @@ static pt_status engine_setup(Engine *s)
     bytes += round256(radix_tiles * 256 * 8);   // radix look-back words
     bytes += round256(8 * 4);                                                      // radix ctl
     bytes += round256((size_t)K * ptk::kDigitStripes * 4 * 256 * 4);               // digit histograms
-    bytes += round256((size_t)K * 4 * 256 * 4) + round256(((size_t)K + 1) * 4);  // digit bases, tile prefix
+    bytes += round256((size_t)K * 4 * 256 * 4) + 2 * round256(((size_t)K + 1) * 4);  // digit bases, tile prefixes
     bytes += round256(((size_t)Bday / 32 + 1) * 4);        // bucket mark bitmap
     bytes += round256(n * 4) * 2;               // infected, infected_inst
     bytes += round256(n / 16 * 2) + round256((ntiles + 1) * 4);  // sweep masks, sweep tile counts
@@ -410,6 +410,7 @@ static pt_status engine_setup(Engine *s)
     d.digit_hist = a.take<int>((size_t)K * ptk::kDigitStripes * 4 * 256);
     d.digit_base = a.take<int>((size_t)K * 4 * 256);
     d.tile_prefix = a.take<int32_t>((size_t)K + 1);
+    d.tile_prefix0 = a.take<int32_t>((size_t)K + 1);
     d.mark = a.take<uint32_t>((size_t)Bday / 32 + 1);
     d.infected = a.take<int32_t>(n);
     d.infected_inst = a.take<int32_t>(n);
