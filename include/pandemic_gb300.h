@@ -193,6 +193,10 @@ typedef struct pt_tuning {
                                    0 integer adds and funnel shifts; 1 the 64-bit adds as
                                    multiply-adds with carry; 2 also the rotations as wide
                                    multiplies (moves work from the ALU to the FMA pipe) */
+    int dense_level;            /* days whose sort reads every schedule key directly instead
+                                   of entries the schedule kernel appends: 0 none; 1, 2, 3
+                                   when the instance's infected are at least a quarter of,
+                                   as many as, twice its buckets */
 } pt_tuning;
 
 /* Sets / reads the launch shapes of sim (allowed before or after pt_setup). */
@@ -283,6 +287,12 @@ pt_status pt_mlp_predict_ensemble(pt_mlp *const *members, int count, const float
 /* The same with x (n x widths[0]) and y (n x widths[layers]) in device memory: no
  * copies and no synchronisation; the work is queued on the first network's stream. */
 pt_status pt_mlp_predict_ensemble_device(pt_mlp *const *members, int count, const float *x, int n, float *y);
+/* Inference (pt_mlp_predict*) runs on the tcgen05 tensor-core kernel by default (BF16
+ * operands in shared memory, FP32 accumulator in tensor memory) when every layer is
+ * at most 256 wide and hidden widths are multiples of 32; enabled = 0 selects the
+ * warp-level mma.sync kernel that training uses.  Both accumulate in FP32 and round
+ * activations to BF16, so they agree to FP32 summation order. */
+pt_status pt_mlp_set_tcgen05(pt_mlp *mlp, int enabled);
 void pt_mlp_destroy(pt_mlp *mlp);
 const char *pt_mlp_last_error(const pt_mlp *mlp);
 

@@ -946,11 +946,10 @@ __global__ void __launch_bounds__(kSweepThreads, 8) k_sweep_count(const InstCons
 }
 
 constexpr int kSweepScanThreads = 1024;
-constexpr int kDenseInfected = 4;   // dense day: kDenseInfected x infected >= the instance's buckets
 
 __global__ void __launch_bounds__(kSweepScanThreads) k_sweep_scan(const InstConst *ic, InstState *is, int K,
                                                                   int32_t *tile_count, int tiles, Scalars *sc,
-                                                                  int day)
+                                                                  int day, int dense_level)
 {
     if (*(volatile const int *)&sc->done) return;
     // exclusive scan in place, a contiguous chunk per thread; entry `tiles` = total
@@ -984,10 +983,12 @@ __global__ void __launch_bounds__(kSweepScanThreads) k_sweep_scan(const InstCons
         }
         const int I = end - start;
         s.infected = I;
-        // Most of today's buckets will be read when the infected (each marks one or two
-        // buckets) number at least a quarter of the buckets: then the sort reads the
-        // schedule keys directly.  Either way the tables are the same.
-        s.dense = (long long)kDenseInfected * I >= (long long)ic[k].bcount[weekend ? 1 : 0] ? 1 : 0;
+        // When the infected (each marks one or two buckets) are many against the
+        // buckets, most buckets will be read, and the sort can read the schedule keys
+        // directly: dense_level 1, 2, 3 take I >= B / 4, I >= B, I >= 2 B; 0 never.
+        // Either way the tables are the same.
+        const long long B = ic[k].bcount[weekend ? 1 : 0];
+        s.dense = dense_level > 0 && 4ll * I >= B * (dense_level == 1 ? 1 : (dense_level == 2 ? 4 : 8)) ? 1 : 0;
         s.infected_per_day[day] = I;
         s.day = day;
         s.days_run = day + 1;
@@ -1060,7 +1061,8 @@ cudaError_t launch_sweep(const DevArrays &d, int day, cudaStream_t s)
     k_sweep_count<<<tiles, kSweepThreads, 0, s>>>(d.ic, d.is, d.tile_inst, d.state, d.sweep_flags, d.sweep_tiles,
                                                   d.sc, day);
     count_launch();
-    k_sweep_scan<<<1, kSweepScanThreads, 0, s>>>(d.ic, d.is, d.K, d.sweep_tiles, tiles, d.sc, day);
+    k_sweep_scan<<<1, kSweepScanThreads, 0, s>>>(d.ic, d.is, d.K, d.sweep_tiles, tiles, d.sc, day,
+                                                 d.tune.dense_level);
     count_launch();
     return cudaGetLastError();
 }

@@ -92,6 +92,8 @@ struct Tuning {
     int radix_blocks_per_sm = 3;    // persistent blocks of a day's radix pass per SM (1..3)
     int sched_tf = 0;               // schedule kernel's Threefry arithmetic: 0 ALU adds and
                                     // shifts, 1 multiply-add adds, 2 also multiply rotations
+    int dense_level = 0;            // when a day's sort reads the schedule keys directly:
+                                    // 0 never; 1, 2, 3: infected >= buckets / 4, x 1, x 2
 };
 
 // Device pointers of a batch of simulations (one simulation is a batch of one).

@@ -156,6 +156,190 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g)
             }
 }
 
+// ---------------------------------------------------------------- tcgen05 inference
+// Forward layers for inference on the fifth-generation tensor cores: tcgen05.mma
+// (kind::f16, BF16 operands, FP32 accumulator in tensor memory), issued by one thread,
+// with both operands K-major in shared memory and the accumulator read back with
+// tcgen05.ld for the bias + GELU epilogue.  One CTA per SM (persistent): it keeps the
+// layer's whole weight matrix (Np x Kp BF16, at most 256 x 256 = 128 KB) in shared
+// memory and walks 128-row tiles of the batch: load the tile (128 x Kp BF16), one
+// MMA per 16 columns of K into a 128 x Np accumulator, epilogue.
+//
+// Shared-memory operand layout (no swizzle, K-major): 8-row x 16-byte core matrices,
+// core (row group g, K group c) at byte (g * KG + c) * 128 with KG = Kp / 8, row r of
+// a core at +16 r.  So the K-direction core stride (the descriptor's leading byte
+// offset) is 128 B and the row-group stride (stride byte offset) is KG * 128 B; the
+// MMA over K columns [16 s, 16 s + 16) starts at +256 s.
+constexpr int kUmmaM = 128;           // rows per tile (the MMA's M)
+constexpr int kUmmaThreads = 128;     // four warps: warp w owns accumulator lanes 32w..32w+31
+constexpr int kUmmaMaxN = 256, kUmmaMaxK = 256;
+constexpr int kUmmaSmem = 1024 + (kUmmaMaxN + kUmmaM) * kUmmaMaxK * 2;   // barrier page + B + A
+constexpr long long kUmmaSpin = 1ll << 22;   // polls of the MMA-completion barrier before giving up
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// tcgen05 shared-memory matrix descriptor: start >> 4 (bits 0-13), leading byte offset
+// >> 4 (16-29), stride byte offset >> 4 (32-45), the fixed 0b001 (46-48), no swizzle.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and B
+// (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 (17-22), M >> 4 (24-28).
+__host__ __device__ constexpr uint32_t umma_idesc(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Copies rows [r0, r0 + R) x Kp BF16 (row stride ld elements) into the core-matrix
+// layout at dst; rows at or past `rows` are zero.
+__device__ __forceinline__ void umma_fill(uint8_t *dst, const bf16 *src, long long ld, int r0, int R, int rows, int Kp)
+{
+    const int KG = Kp / 8, chunks = R * KG;
+    for (int q = threadIdx.x; q < chunks; q += blockDim.x) {
+        const int r = q / KG, c = q % KG;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (r0 + r < rows) v = *reinterpret_cast<const uint4 *>(src + (long long)(r0 + r) * ld + 8 * c);
+        *reinterpret_cast<uint4 *>(dst + ((r >> 3) * KG + c) * 128 + (r & 7) * 16) = v;
+    }
+}
+
+// One layer: out = act(A W^T + bias) over M rows.  A: M x Kp BF16 (row stride lda);
+// W: Np x Kp BF16 (zero rows past N); Kp a multiple of 16, Np of 16, both <= 256.
+// Hidden layers (H set) store BF16 activations (row stride ldh); the last layer
+// (Z set) stores FP32 outputs (row stride N).  error: set when a wait gives up.
+__global__ void __launch_bounds__(kUmmaThreads, 1)
+    k_umma_layer(const bf16 *A, long long lda, int M, int Kp, const bf16 *W, int Np, int N, const float *bias, int gelu,
+                 bf16 *H, long long ldh, float *Z, int *error)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + 64);
+    uint8_t *sB = smem + 1024;
+    uint8_t *sA = sB + (size_t)Np * Kp * 2;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tmem_slot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    umma_fill(sB, W, Kp, 0, Np, Np, Kp);
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t KG = (uint32_t)Kp / 8;
+    const uint32_t idesc = umma_idesc(kUmmaM, Np);
+    const int tiles = (M + kUmmaM - 1) / kUmmaM;
+    uint32_t phase = 0;
+    bool failed = false;
+    for (int t = blockIdx.x; t < tiles && !failed; t += gridDim.x) {
+        const int m0 = t * kUmmaM;
+        umma_fill(sA, A, lda, m0, kUmmaM, M, Kp);
+        asm volatile("fence.proxy.async.shared::cta;");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (threadIdx.x == 0) {
+            const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+            for (int s = 0; s < Kp / 16; s++) {
+                const uint64_t ad = umma_desc(a0 + 256u * s, 128u, KG * 128u);
+                const uint64_t bd = umma_desc(b0 + 256u * s, 128u, KG * 128u);
+                const uint32_t acc = s > 0 ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_u32(bar)));
+        }
+        // wait for the MMAs (bounded; the outcome is made uniform over the block)
+        long long spins = 0;
+        uint32_t done = 0;
+        while (!done) {
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(done)
+                : "r"(smem_u32(bar)), "r"(phase));
+            if (!done && ++spins > kUmmaSpin) break;
+        }
+        if (__syncthreads_or(!done)) {
+            if (threadIdx.x == 0) atomicExch(error, 1);
+            failed = true;
+            break;
+        }
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        // epilogue: warp w reads accumulator lanes (rows) 32w..32w+31, 32 columns at a time
+        const int row = m0 + 32 * warp + lane;
+        for (int c0 = 0; c0 < Np; c0 += 32) {
+            uint32_t v[32];
+            const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+                  "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+                  "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+                  "=r"(v[30]), "=r"(v[31])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            if (row >= M) continue;
+            if (H) {
+                uint32_t packed[16];
+#pragma unroll
+                for (int j = 0; j < 32; j += 2) {
+                    const int c = c0 + j;
+                    float z0 = __uint_as_float(v[j]) + (c < N ? bias[c] : 0.f);
+                    float z1 = __uint_as_float(v[j + 1]) + (c + 1 < N ? bias[c + 1] : 0.f);
+                    if (gelu) {
+                        z0 = 0.5f * z0 * (1.f + erff(z0 * 0.70710678118654752f));
+                        z1 = 0.5f * z1 * (1.f + erff(z1 * 0.70710678118654752f));
+                    }
+                    packed[j / 2] = pack2(__float2bfloat16(z0), __float2bfloat16(z1));
+                }
+                // N is a multiple of 32 for hidden layers: whole 64-byte runs
+                uint4 *dst = reinterpret_cast<uint4 *>(H + (long long)row * ldh + c0);
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    dst[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+            } else {
+                float *dst = Z + (long long)row * N;
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    const int c = c0 + j;
+                    if (c < N) dst[c] = __uint_as_float(v[j]) + bias[c];
+                }
+            }
+        }
+        // the next tile's MMA overwrites the accumulator and its fill the A operand
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+    }
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+}
+
+// Zero-padded BF16 copies for the tcgen05 path: src rows x cols (row stride cols) ->
+// dst prow x pcol.
+__global__ void k_pad_bf16(const bf16 *src, int rows, int cols, bf16 *dst, int prow, int pcol)
+{
+    const long long n = (long long)prow * pcol;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(i / pcol), c = (int)(i % pcol);
+        dst[i] = (r < rows && c < cols) ? src[(long long)r * cols + c] : __float2bfloat16(0.f);
+    }
+}
+
 // rows of the data set -> a BF16 input batch and an FP32 target batch
 __global__ void k_gather(const float *X, const float *Y, const int *idx, int B, int din, int dout, bf16 *Hb,
                          float *Yb)
@@ -249,6 +433,14 @@ struct pt_mlp {
     long long step = 0;
     std::string err;
     std::vector<void *> allocs;
+    // tcgen05 inference: zero-padded BF16 copies of the weights (rows and columns to
+    // multiples of 16), the padded input batch, and a wait error word
+    int use_umma = 1;
+    bool packed_stale = true;
+    std::vector<bf16 *> wpk;
+    std::vector<int> kpad, npad;
+    bf16 *h0p = nullptr;
+    int *umma_err = nullptr;
 };
 
 static pt_status mfail(pt_mlp *m, pt_status st, const std::string &msg)
@@ -359,6 +551,98 @@ static cudaError_t backward(pt_mlp *m, int B)
 
 static int grid_for(long long n) { return (int)std::min<long long>((n + 255) / 256, 4096); }
 
+static int pad16(int x) { return (x + 15) / 16 * 16; }
+
+// The tcgen05 path takes every layer whose padded sizes fit the kernel: inputs and
+// outputs at most 256 wide, hidden widths a multiple of 32.
+static bool umma_fits(const pt_mlp *m)
+{
+    for (int l = 0; l < m->L; l++) {
+        const int din = m->width[l], dout = m->width[l + 1];
+        if (pad16(din) > kUmmaMaxK || pad16(dout) > kUmmaMaxN) return false;
+        if (l > 0 && din % 16 != 0) return false;           // read in place from H[l]
+        if (l + 1 < m->L && dout % 32 != 0) return false;  // whole 64-byte output runs
+    }
+    return true;
+}
+
+static int sm_count_mlp()
+{
+    static const int n = [] {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 1;
+    }();
+    return n;
+}
+
+// forward pass for inference over the B rows in H[0]: tcgen05 layers when the shapes
+// fit (Z[L-1] receives the outputs, hidden H[l] the activations), else forward().
+static cudaError_t forward_infer(pt_mlp *m, int B)
+{
+    if (!m->use_umma || !umma_fits(m)) return forward(m, B);
+    cudaError_t e = cudaSuccess;
+    if (m->wpk.empty()) {
+        static const cudaError_t attr =
+            cudaFuncSetAttribute(k_umma_layer, cudaFuncAttributeMaxDynamicSharedMemorySize, kUmmaSmem);
+        if (attr != cudaSuccess) return attr;
+        for (int l = 0; l < m->L; l++) {
+            m->kpad.push_back(pad16(m->width[l]));
+            m->npad.push_back(pad16(m->width[l + 1]));
+            bf16 *p = nullptr;
+            e = dalloc(m, &p, (size_t)m->kpad[l] * m->npad[l]);
+            if (e != cudaSuccess) return e;
+            m->wpk.push_back(p);
+        }
+        e = dalloc(m, &m->h0p, (size_t)m->max_batch * m->kpad[0]);
+        if (e == cudaSuccess) e = dalloc(m, &m->umma_err, 1);
+        if (e == cudaSuccess) e = cudaMemsetAsync(m->umma_err, 0, sizeof(int), m->stream);
+        if (e != cudaSuccess) return e;
+        m->packed_stale = true;
+    }
+    if (m->packed_stale) {
+        for (int l = 0; l < m->L; l++)
+            k_pad_bf16<<<grid_for((long long)m->npad[l] * m->kpad[l]), 256, 0, m->stream>>>(
+                m->wb + m->woff[l], m->width[l + 1], m->width[l], m->wpk[l], m->npad[l], m->kpad[l]);
+        m->packed_stale = false;
+    }
+    k_pad_bf16<<<grid_for((long long)B * m->kpad[0]), 256, 0, m->stream>>>(m->H[0], B, m->width[0], m->h0p, B,
+                                                                           m->kpad[0]);
+    const int tiles = (B + kUmmaM - 1) / kUmmaM;
+    for (int l = 0; l < m->L; l++) {
+        const int Kp = m->kpad[l], Np = m->npad[l];
+        const bool last = l + 1 == m->L;
+        // at least 80 KB per CTA: two CTAs per SM at most, within the 512 TMEM columns
+        const int smem = std::max(1024 + (Np + kUmmaM) * Kp * 2, 80 * 1024);
+        const int per_sm = smem > 114 * 1024 ? 1 : 2;
+        const int grid = std::max(1, std::min(tiles, per_sm * sm_count_mlp()));
+        const bf16 *A = l == 0 ? m->h0p : m->H[l];
+        const long long lda = l == 0 ? m->kpad[0] : m->width[l];
+        k_umma_layer<<<grid, kUmmaThreads, smem, m->stream>>>(A, lda, B, Kp, m->wpk[l], Np, m->width[l + 1],
+                                                             m->w + m->boff[l], last ? 0 : 1,
+                                                             last ? nullptr : m->H[l + 1], m->width[l + 1],
+                                                             last ? m->Z[l] : nullptr, m->umma_err);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// A device wait of the tcgen05 path that gave up: reported once, then cleared.
+static pt_status umma_check(pt_mlp *m)
+{
+    if (!m->umma_err) return PT_OK;
+    int h = 0;
+    MCK(cudaMemcpyAsync(&h, m->umma_err, sizeof(int), cudaMemcpyDeviceToHost, m->stream), "tcgen05 error word");
+    MCK(cudaStreamSynchronize(m->stream), "sync");
+    if (h) {
+        cudaMemsetAsync(m->umma_err, 0, sizeof(int), m->stream);
+        return mfail(m, PT_ERR_TIMEOUT, "a tcgen05 MMA completion wait gave up");
+    }
+    return PT_OK;
+}
+
 extern "C" {
 
 pt_status pt_mlp_create(int layers, const int *widths, int max_batch, uint64_t seed, void *cuda_stream, pt_mlp **out)
@@ -434,6 +718,7 @@ pt_status pt_mlp_set_params(pt_mlp *m, const float *params)
     MCK(cudaGetLastError(), "bf16 weights");
     MCK(cudaStreamSynchronize(m->stream), "sync");
     m->step = 0;
+    m->packed_stale = true;
     return PT_OK;
 }
 
@@ -487,6 +772,7 @@ pt_status pt_mlp_train(pt_mlp *m, int epochs, int batch, float lr, uint64_t shuf
             MCK(forward(m, B), "forward");
             MCK(backward(m, B), "backward");
             m->step++;
+            m->packed_stale = true;
             const float c1 = 1.f - std::pow(0.9f, (float)m->step), c2 = 1.f - std::pow(0.999f, (float)m->step);
             k_adam<<<grid_for(m->nparam), 256, 0, m->stream>>>(m->w, m->m, m->v, m->grad, m->wb, m->nparam, lr, 0.9f,
                                                                0.999f, 1e-8f, c1, c2);
@@ -547,7 +833,7 @@ pt_status pt_mlp_predict(pt_mlp *m, const float *X, int n, float *Y)
                             m->stream);
         if (e != cudaSuccess) break;
         k_gather<<<B, 128, 0, m->stream>>>(dX, nullptr, nullptr, B, din, dout, m->H[0], nullptr);
-        e = forward(m, B);
+        e = forward_infer(m, B);
         if (e != cudaSuccess) break;
         e = cudaMemcpyAsync(Y + (size_t)s0 * dout, m->Z[m->L - 1], (size_t)B * dout * sizeof(float),
                             cudaMemcpyDeviceToHost, m->stream);
@@ -555,6 +841,13 @@ pt_status pt_mlp_predict(pt_mlp *m, const float *X, int n, float *Y)
     if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
     cudaFree(dX);
     MCK(e, "predict");
+    return umma_check(m);
+}
+
+pt_status pt_mlp_set_tcgen05(pt_mlp *m, int enabled)
+{
+    if (!m) return PT_ERR_ARG;
+    m->use_umma = enabled ? 1 : 0;
     return PT_OK;
 }
 
@@ -589,7 +882,7 @@ pt_status pt_mlp_predict_ensemble(pt_mlp *const *members, int count, const float
             const cudaStream_t own = q->stream;
             q->stream = s;
             k_gather<<<B, 128, 0, s>>>(dX, nullptr, nullptr, B, din, dout, q->H[0], nullptr);
-            e = forward(q, B);
+            e = forward_infer(q, B);
             if (e == cudaSuccess) {
                 const long long total = (long long)B * dout;
                 k_accumulate<<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, s>>>(
@@ -606,6 +899,10 @@ pt_status pt_mlp_predict_ensemble(pt_mlp *const *members, int count, const float
     cudaFree(dX);
     if (acc) cudaFree(acc);
     MCK(e, "ensemble predict");
+    for (int j = 0; j < count; j++) {
+        const pt_status st = umma_check(members[j]);
+        if (st != PT_OK) return st;
+    }
     return PT_OK;
 }
 
@@ -634,7 +931,7 @@ pt_status pt_mlp_predict_ensemble_device(pt_mlp *const *members, int count, cons
             const cudaStream_t own = q->stream;
             q->stream = s;
             k_gather<<<B, 128, 0, s>>>(X + (size_t)s0 * din, nullptr, nullptr, B, din, dout, q->H[0], nullptr);
-            cudaError_t e = forward(q, B);
+            cudaError_t e = forward_infer(q, B);
             if (e == cudaSuccess) {
                 const long long total = (long long)B * dout;
                 k_accumulate<<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, s>>>(

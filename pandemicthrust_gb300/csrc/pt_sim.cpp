@@ -839,6 +839,7 @@ static pt_tuning to_public(const ptk::Tuning &t)
     o.infect_blocks_per_sm = t.infect_blocks_per_sm;
     o.radix_blocks_per_sm = t.radix_blocks_per_sm;
     o.sched_tf = t.sched_tf;
+    o.dense_level = t.dense_level;
     return o;
 }
 
@@ -846,15 +847,17 @@ static pt_status engine_set_tuning(Engine *s, const pt_tuning *t)
 {
     if (!t || (t->infect_coop != 0 && t->infect_coop != 1) || t->infect_blocks_per_sm < 1 ||
         t->infect_blocks_per_sm > 32 || t->radix_blocks_per_sm < 1 || t->radix_blocks_per_sm > 3 ||
-        t->sched_tf < 0 || t->sched_tf > 2)
+        t->sched_tf < 0 || t->sched_tf > 2 || t->dense_level < 0 || t->dense_level > 3)
         return fail(s, PT_ERR_ARG, "launch shape outside its range");
     ptk::Tuning n;
     n.infect_coop = t->infect_coop;
     n.infect_blocks_per_sm = t->infect_blocks_per_sm;
     n.radix_blocks_per_sm = t->radix_blocks_per_sm;
     n.sched_tf = t->sched_tf;
+    n.dense_level = t->dense_level;
     if (n.infect_coop != s->d.tune.infect_coop || n.infect_blocks_per_sm != s->d.tune.infect_blocks_per_sm ||
-        n.radix_blocks_per_sm != s->d.tune.radix_blocks_per_sm || n.sched_tf != s->d.tune.sched_tf) {
+        n.radix_blocks_per_sm != s->d.tune.radix_blocks_per_sm || n.sched_tf != s->d.tune.sched_tf ||
+        n.dense_level != s->d.tune.dense_level) {
         // the captured day loop holds the old launch shapes
         if (s->stream) cudaStreamSynchronize(s->stream);
         if (s->run_graph) cudaGraphExecDestroy(s->run_graph);
@@ -877,6 +880,7 @@ static std::vector<long long> tune_key(const Engine *s)
 // The tuner.  The infection, radix and schedule stages are timed separately (per-stage
 // CUDA events around every day), so one run measures one candidate of each: run i
 // uses infection candidate i, radix candidate i % 3 and Threefry form (i + 1) % 3.
+// Two more runs then try the dense-day sort levels 2 and 3 with the shapes chosen.
 static pt_status engine_autotune(Engine *s, int days, pt_tuning *chosen)
 {
     if (!s->setup_done) return fail(s, PT_ERR_STATE, "autotune before setup");
@@ -908,6 +912,7 @@ static pt_status engine_autotune(Engine *s, int days, pt_tuning *chosen)
         t.infect_blocks_per_sm = infect[i].bps;
         t.radix_blocks_per_sm = radix[i % 3];
         t.sched_tf = tfs[(i + 1) % 3];
+        t.dense_level = 0;
         pt_status st = engine_set_tuning(s, &t);
         if (st == PT_OK) st = engine_reset(s);
         if (st == PT_OK) st = engine_set_timing(s, 1);
@@ -938,6 +943,29 @@ static pt_status engine_autotune(Engine *s, int days, pt_tuning *chosen)
     t.infect_blocks_per_sm = infect[best_i].bps;
     t.radix_blocks_per_sm = radix[rbest];
     t.sched_tf = tfs[tbest];
+    t.dense_level = 0;
+    // the dense-day sort changes both the schedule and the sort stage: its levels are
+    // timed after the others are chosen, against their schedule + sort time
+    float best_dense = best_rad[rbest] + best_tf[tbest];
+    for (int lv = 2; lv <= 3; lv++) {
+        pt_tuning c = t;
+        c.dense_level = lv;
+        pt_status st = engine_set_tuning(s, &c);
+        if (st == PT_OK) st = engine_reset(s);
+        if (st == PT_OK) st = engine_set_timing(s, 1);
+        if (st != PT_OK) return st;
+        s->max_days = trial;
+        st = engine_run(s);
+        s->max_days = saved_max;
+        if (st != PT_OK) return st;
+        float ms[16];
+        engine_stage_ms(s, ms, nullptr);
+        const float cost = ms[kStRadix] + ms[8 + kStRadix] + ms[kStSchedule] + ms[8 + kStSchedule];
+        if (cost < best_dense) {
+            best_dense = cost;
+            t.dense_level = lv;
+        }
+    }
     pt_status st = engine_set_timing(s, 0);
     if (st == PT_OK) st = engine_set_tuning(s, &t);
     if (st == PT_OK) st = engine_reset(s);

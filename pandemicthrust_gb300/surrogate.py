@@ -66,6 +66,7 @@ class MLP:
         lib.pt_mlp_predict.argtypes = [vp, fp, ctypes.c_int, fp]
         lib.pt_mlp_predict_ensemble.argtypes = [ctypes.POINTER(vp), ctypes.c_int, fp, ctypes.c_int, fp]
         lib.pt_mlp_predict_ensemble_device.argtypes = [ctypes.POINTER(vp), ctypes.c_int, vp, ctypes.c_int, vp]
+        lib.pt_mlp_set_tcgen05.argtypes = [vp, ctypes.c_int]
         lib.pt_mlp_destroy.argtypes = [vp]
         lib.pt_mlp_last_error.argtypes = [vp]
         lib.pt_mlp_last_error.restype = ctypes.c_char_p
@@ -124,6 +125,10 @@ class MLP:
         Y = np.zeros((len(X), self.widths[-1]), np.float32)
         self._check(self.lib.pt_mlp_predict(self.h, self._f(X), len(X), self._f(Y)))
         return Y
+
+    def set_tcgen05(self, enabled=True):
+        """Inference on the tcgen05 kernel (default) or on the mma.sync kernel training uses."""
+        self._check(self.lib.pt_mlp_set_tcgen05(self.h, 1 if enabled else 0))
 
     def close(self):
         if getattr(self, "h", None):
