@@ -414,6 +414,7 @@ def run_batched(args, pt, torch, stream, local):
     sp = ctypes.c_void_p(stream.cuda_stream)
     b = pt.PandemicBatch(params, seeds, stream=sp)
     b.setup()
+    tuning = b.autotune()   # launch shapes for this batch (part of the warm-up)
     K, persons, padded = b.size()
     sizes = [b.info(k)["number_people"] for k in range(K)]
     for _ in range(args.batch_warmup):
@@ -465,6 +466,7 @@ def run_batched(args, pt, torch, stream, local):
     e0.record(stream)
     b2 = pt.PandemicBatch(params, seeds, stream=sp)
     b2.setup()
+    b2.autotune()   # the shapes chosen above for this batch size (cached: no timing runs)
     b2.run()
     b2.final_gen_counts()
     e2e_pd = sum(n * int(d) for n, d in zip(sizes, b2.days_run()))
@@ -511,6 +513,7 @@ def run_batched(args, pt, torch, stream, local):
         "warmup": args.batch_warmup, "ms_per_step": ms / args.batch_steps,
         "days_run": {"min": int(min(days)), "max": int(max(days)), "mean": float(sum(days)) / K},
         "gpu_launches": launches,
+        "tuning": tuning,
         "stages": breakdown,
         "infected_fraction_mean": infected_days / max(float(sum(n * int(d) for n, d in zip(sizes, days))), 1.0),
         "e2e": {"value": e2e_pd / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -695,6 +698,7 @@ def main():
     N, L = info["number_people"], info["number_workplaces"]
     Bc_wd = 2 * (L - info["type_offset"][8])
     Bc_we = 10 * (L - info["type_offset"][9])
+    tuning = sim.autotune()   # launch shapes (untimed, before the warm-up)
 
     # warm-up steps (untimed)
     for _ in range(args.warmup):
@@ -789,6 +793,7 @@ def main():
         for _ in range(args.e2e_steps):
             s2 = pt.PandemicSim(params, seed, stream=ctypes.c_void_p(stream.cuda_stream))
             s2.setupSim()
+            s2.autotune()   # the shapes chosen above for this size (cached: no timing runs)
             c2, i2 = s2.runToCompletion()
             s2.final_gen_counts()
             e2e_days += len(i2)
@@ -837,6 +842,7 @@ def main():
                        "batched_instances_vs_alone": batched.get("parity") if batched else None},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
+            "tuning": tuning,
             "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic},
             "int_roofline": int_roof(dominant, nwd, nwe),

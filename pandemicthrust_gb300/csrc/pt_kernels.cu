@@ -1227,8 +1227,10 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wl = warp * kSchedWarpPersons;      // the warp's first person, tile numbering
     constexpr int kRounds = WEEKEND ? 16 : 8;
-    constexpr int kBits = WEEKEND ? 2 : 3;  // marked entries per lane and round: <= 3 / <= 4
-    uint32_t cpack = 0;
+    // which of the lane's entries are marked: bit 3j + k (weekend) / 4j + k (weekday) of
+    // round j, kept for the append phase
+    constexpr int kPer = WEEKEND ? 3 : 4;
+    unsigned long long mbits = 0;
     int mine = 0;
     if (WEEKEND) {
         // kernel_assignWeekendErrands (PandemicSim.cu:2082-2094): counters E0 + 2p, E0 + 2p + 1
@@ -1251,7 +1253,7 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
             const int cnt = (int)mk[0] + (int)mk[1] + (int)mk[2];
 #pragma unroll
             for (int k = 0; k < 3; k++) digit_count(s_dh, passes, mk[k], kb[k] - (uint32_t)bb);
-            cpack |= (uint32_t)cnt << (kBits * j);
+            mbits |= (unsigned long long)((uint32_t)mk[0] | ((uint32_t)mk[1] << 1) | ((uint32_t)mk[2] << 2)) << (kPer * j);
             mine += cnt;
         }
     } else {
@@ -1281,7 +1283,8 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
             const int cnt = (int)mk[0] + (int)mk[1] + (int)mk[2] + (int)mk[3];
 #pragma unroll
             for (int k = 0; k < 4; k++) digit_count(s_dh, passes, mk[k], kb[k] - (uint32_t)bb);
-            cpack |= (uint32_t)cnt << (kBits * j);
+            mbits |= (unsigned long long)((uint32_t)mk[0] | ((uint32_t)mk[1] << 1) | ((uint32_t)mk[2] << 2) |
+                                          ((uint32_t)mk[3] << 3)) << (kPer * j);
             mine += cnt;
         }
     }
@@ -1332,11 +1335,11 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
     cvals += ic[inst].kbase;
     // append the marked entries, rounds in order, lanes in order within a round
     int run = s_wbase[warp];
-    const uint32_t cmask = (1u << kBits) - 1u;
     const int gbase = pbase + tbase;   // global id of the tile's first person
 #pragma unroll 1
     for (int j = 0; j < kRounds; j++) {
-        const int cnt = (int)((cpack >> (kBits * j)) & cmask);
+        const uint32_t bits = (uint32_t)(mbits >> (kPer * j)) & ((1u << kPer) - 1u);
+        const int cnt = __popc(bits);
         if (__ballot_sync(0xffffffffu, cnt > 0) == 0) continue;
         const int incl = warp_inclusive_scan(cnt);
         int pos = run + incl - cnt;
@@ -1345,27 +1348,21 @@ __global__ void __launch_bounds__(kSchedThreads, 8) k_sched(const InstConst *ic,
                 const int i = wl + 32 * j + lane;
 #pragma unroll
                 for (int k = 0; k < 3; k++) {
-                    const uint32_t b = (uint32_t)kk[3 * (size_t)(tbase + i) + k];
-                    if (is_marked(mark, (int)b)) {
-                        ckeys[pos] = b - (uint32_t)bb;
+                    if ((bits >> k) & 1u) {
+                        ckeys[pos] = (uint32_t)kk[3 * (size_t)(tbase + i) + k] - (uint32_t)bb;
                         cvals[pos] = (uint32_t)(gbase + i);
                         pos++;
                     }
                 }
             } else {
+                // entry k of the round: person i + k / 2, hour k % 2
                 const int i = wl + 64 * j + 2 * lane;
 #pragma unroll
-                for (int k = 0; k < 2; k++) {
-                    if (i + k < valid) {
-#pragma unroll
-                        for (int h = 0; h < 2; h++) {
-                            const uint32_t b = (uint32_t)kk[(size_t)h * NK + tbase + i + k];
-                            if (is_marked(mark, (int)b)) {
-                                ckeys[pos] = b - (uint32_t)bb;
-                                cvals[pos] = (uint32_t)(gbase + i + k);
-                                pos++;
-                            }
-                        }
+                for (int k = 0; k < 4; k++) {
+                    if ((bits >> k) & 1u) {
+                        ckeys[pos] = (uint32_t)kk[(size_t)(k & 1) * NK + tbase + i + (k >> 1)] - (uint32_t)bb;
+                        cvals[pos] = (uint32_t)(gbase + i + (k >> 1));
+                        pos++;
                     }
                 }
             }

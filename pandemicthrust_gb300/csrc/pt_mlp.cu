@@ -6,10 +6,11 @@
 // width[l], row-major) then b_l (width[l+1]); a BF16 copy of every weight feeds the
 // tensor cores.  The library owns all device memory; callers pass host arrays.
 //
-// GEMMs are small (at most a few thousand rows by 256), so they run on the warp-level
-// tensor-core instruction mma.sync m16n8k16 (BF16 in, FP32 accumulate): one kernel
-// with strided operands serves the forward product X W^T, the data gradient dZ W and
-// the weight gradient dZ^T X.
+// Training GEMMs are small (a minibatch of a few hundred rows by 256) and need
+// transposed operands, so they run on the warp-level tensor-core instruction mma.sync
+// m16n8k16 (BF16 in, FP32 accumulate): one kernel with strided operands serves the
+// forward product X W^T, the data gradient dZ W and the weight gradient dZ^T X.
+// Inference over large batches runs every layer on tcgen05.mma (k_umma_layer below).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -171,7 +172,8 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g)
 // offset) is 128 B and the row-group stride (stride byte offset) is KG * 128 B; the
 // MMA over K columns [16 s, 16 s + 16) starts at +256 s.
 constexpr int kUmmaM = 128;           // rows per tile (the MMA's M)
-constexpr int kUmmaThreads = 128;     // four warps: warp w owns accumulator lanes 32w..32w+31
+constexpr int kUmmaThreads = 256;     // eight warps: warp w reads accumulator lanes 32 (w % 4).. + 31,
+                                      // the 32-column chunks of parity w / 4
 constexpr int kUmmaMaxN = 256, kUmmaMaxK = 256;
 constexpr int kUmmaSmem = 1024 + (kUmmaMaxN + kUmmaM) * kUmmaMaxK * 2;   // barrier page + B + A
 constexpr long long kUmmaSpin = 1ll << 22;   // polls of the MMA-completion barrier before giving up
@@ -194,17 +196,23 @@ __host__ __device__ constexpr uint32_t umma_idesc(int M, int N)
 }
 
 // Copies rows [r0, r0 + R) x Kp BF16 (row stride ld elements) into the core-matrix
-// layout at dst; rows at or past `rows` are zero.
+// layout at dst with asynchronous 16-byte copies (every thread issues all of its
+// copies before waiting, so the whole tile is in flight at once); rows at or past
+// `rows` are zero-filled.  The caller waits with umma_fill_wait.
 __device__ __forceinline__ void umma_fill(uint8_t *dst, const bf16 *src, long long ld, int r0, int R, int rows, int Kp)
 {
     const int KG = Kp / 8, chunks = R * KG;
     for (int q = threadIdx.x; q < chunks; q += blockDim.x) {
         const int r = q / KG, c = q % KG;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (r0 + r < rows) v = *reinterpret_cast<const uint4 *>(src + (long long)(r0 + r) * ld + 8 * c);
-        *reinterpret_cast<uint4 *>(dst + ((r >> 3) * KG + c) * 128 + (r & 7) * 16) = v;
+        const bool in = r0 + r < rows;
+        const bf16 *g = in ? src + (long long)(r0 + r) * ld + 8 * c : src;
+        const uint32_t s = smem_u32(dst + ((r >> 3) * KG + c) * 128 + (r & 7) * 16);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(s), "l"(g), "r"(in ? 16 : 0) : "memory");
     }
+    asm volatile("cp.async.commit_group;" ::: "memory");
 }
+
+__device__ __forceinline__ void umma_fill_wait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // One layer: out = act(A W^T + bias) over M rows.  A: M x Kp BF16 (row stride lda);
 // W: Np x Kp BF16 (zero rows past N); Kp a multiple of 16, Np of 16, both <= 256.
@@ -228,8 +236,7 @@ __global__ void __launch_bounds__(kUmmaThreads, 1)
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
-    umma_fill(sB, W, Kp, 0, Np, Np, Kp);
-    asm volatile("fence.proxy.async.shared::cta;");
+    umma_fill(sB, W, Kp, 0, Np, Np, Kp);   // waited for with the first tile's fill
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
@@ -242,6 +249,7 @@ __global__ void __launch_bounds__(kUmmaThreads, 1)
     for (int t = blockIdx.x; t < tiles && !failed; t += gridDim.x) {
         const int m0 = t * kUmmaM;
         umma_fill(sA, A, lda, m0, kUmmaM, M, Kp);
+        umma_fill_wait();
         asm volatile("fence.proxy.async.shared::cta;");
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();
@@ -277,11 +285,13 @@ __global__ void __launch_bounds__(kUmmaThreads, 1)
         }
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;");
-        // epilogue: warp w reads accumulator lanes (rows) 32w..32w+31, 32 columns at a time
-        const int row = m0 + 32 * warp + lane;
-        for (int c0 = 0; c0 < Np; c0 += 32) {
+        // epilogue: warp w reads accumulator lanes (rows) 32 (w % 4) .. + 31, 32 columns at
+        // a time, the chunks of parity w / 4
+        const int quarter = warp & 3;
+        const int row = m0 + 32 * quarter + lane;
+        for (int c0 = 32 * (warp >> 2); c0 < Np; c0 += 64) {
             uint32_t v[32];
-            const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
+            const uint32_t taddr = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)c0;
             asm volatile(
                 "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
                 "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"

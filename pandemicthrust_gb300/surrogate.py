@@ -516,11 +516,12 @@ SEARCH_R = (1.5, 1.2)
 SEARCH_SEEDS_PER_MILLION = 20
 
 
-def search_scenarios(n, rng, budget_days):
+def search_scenarios(n, rng, budget_days, vaccination=0.2):
     """n intervention scenarios for the search: R fixed at SEARCH_R, seeds fixed (per
-    million persons; the surrogate takes them in its own population's numbers),
-    closure start uniform in its range, closure length uniform in [0, budget_days],
-    absenteeism and vaccination uniform in their ranges."""
+    million persons; the surrogate takes them in its own population's numbers), the
+    vaccination coverage fixed (the doses at hand), closure start uniform in its
+    range, closure length uniform in [0, budget_days], absenteeism uniform in its
+    range."""
     lo, hi = RANGES["closure_start"]
     out = []
     for _ in range(n):
@@ -529,7 +530,7 @@ def search_scenarios(n, rng, budget_days):
             "closure_start": int(rng.integers(lo, hi + 1)),
             "closure_days": int(rng.integers(0, budget_days + 1)),
             "absenteeism": float(rng.uniform(*RANGES["absenteeism"])),
-            "vaccination": float(rng.uniform(*RANGES["vaccination"])),
+            "vaccination": float(vaccination),
         })
     return out
 
@@ -556,7 +557,8 @@ def transfer(pred, persons, model_persons):
 
 
 def search(surrogate, persons=50_000_000, candidates=100_000, budget_days=28, top_fraction=0.01, judge_top=None,
-           replicates=32, seed=2026, seed_base=300_000_000, max_persons_per_batch=700_000_000):
+           replicates=32, seed=2026, seed_base=300_000_000, max_persons_per_batch=700_000_000, vaccination=0.2,
+           min_attack=1e-3):
     """Surrogate-screened intervention search.
 
     Scores `candidates` random intervention scenarios with the surrogate (minimal
@@ -565,9 +567,11 @@ def search(surrogate, persons=50_000_000, candidates=100_000, budget_days=28, to
     them) with `replicates` runs each at `persons` on the batched simulator, which
     judges the surrogate (peak height and attack rate errors against the replicate
     mean) and makes the final choice (the fallback: the simulator's best, not the
-    surrogate's, is returned).  Returns a dict of the timings, errors and choices."""
+    surrogate's, is returned).  Errors count (scenario, strain) pairs whose simulated
+    attack rate is at least min_attack (0.1% is 50,000 persons at 50M).  Returns a dict
+    of the timings, errors and choices."""
     rng = np.random.default_rng(seed)
-    scen = search_scenarios(candidates, rng, budget_days)
+    scen = search_scenarios(candidates, rng, budget_days, vaccination)
     X = features(scen)
     surrogate.raw_features(X[:min(len(X), 4096)])   # warm-up
     t0 = time.time()
@@ -584,19 +588,20 @@ def search(surrogate, persons=50_000_000, candidates=100_000, budget_days=28, to
     t_sim = time.time() - t0
     truth = truth_summary(sim)
     sub = {k: np.asarray(v)[judged] for k, v in pred.items()}
-    pk, at = relative_errors(predicted_summary(sub), truth)
+    pk, at = relative_errors(predicted_summary(sub), truth, min_attack)
     person_days = float((sim["persons"] * sim["days"]).sum())
     abm_score = truth["attack"].sum(axis=1)
     best_abm = int(np.argmin(abm_score))
     return {
         "persons": int(sim["persons"].mean()), "candidates": candidates, "budget_closure_days": budget_days,
+        "vaccination": vaccination,
         "top": int(len(top)), "judged": int(len(judged)), "replicates": replicates,
         "surrogate_scenarios_per_s": candidates / t_score, "surrogate_seconds": t_score,
         "abm_seconds": t_sim, "abm_runs": int(len(judged) * replicates),
         "abm_person_days_per_s": person_days / t_sim,
         "error": {"peak_height_median": float(np.median(pk)), "peak_height_mean": float(np.mean(pk)),
                   "attack_rate_median": float(np.median(at)), "attack_rate_mean": float(np.mean(at)),
-                  "pairs": int(len(pk)), "min_attack": 0.01},
+                  "pairs": int(len(pk)), "min_attack": min_attack},
         "surrogate_choice": dict(scen[int(judged[0])], predicted_attack=[float(x) for x in pred["attack"][judged[0]]],
                                  simulated_attack=[float(x) for x in truth["attack"][0]]),
         "abm_choice": dict(scen[int(judged[best_abm])], simulated_attack=[float(x) for x in truth["attack"][best_abm]]),
@@ -634,6 +639,11 @@ def main(argv=None):
     e.add_argument("--replicates", type=int, default=32)
     e.add_argument("--seed", type=int, default=99)
     e.add_argument("--seed-base", type=int, default=70_000_000)
+    f = sub.add_parser("infer", help="time ensemble inference on random scenarios (no simulation)")
+    f.add_argument("--model", default=SHIPPED_MODEL)
+    f.add_argument("--rows", type=int, default=262144)
+    f.add_argument("--repeats", type=int, default=3)
+    f.add_argument("--mma-sync", action="store_true", help="the mma.sync kernel instead of tcgen05")
     q = sub.add_parser("search")
     q.add_argument("--model", default=SHIPPED_MODEL)
     q.add_argument("--persons", type=int, default=50_000_000)
@@ -661,6 +671,19 @@ def main(argv=None):
         s.save(a.out, **info)
         s.close()
         print(json.dumps(info))
+    elif a.cmd == "infer":
+        s = Surrogate.load(a.model, max_batch=65536)
+        for net in s.nets:
+            net.set_tcgen05(not a.mma_sync)
+        X = features(sample_scenarios(a.rows, np.random.default_rng(5)))
+        times = []
+        for _ in range(a.repeats):
+            t0 = time.time()
+            s.raw_features(X)
+            times.append(time.time() - t0)
+        s.close()
+        print(json.dumps({"rows": a.rows, "members": len(s.nets), "kernel": "mma.sync" if a.mma_sync else "tcgen05",
+                          "seconds": times, "scenarios_per_s": a.rows / min(times)}))
     elif a.cmd == "search":
         s = Surrogate.load(a.model, max_batch=65536)
         r = search(s, a.persons, a.candidates, a.budget_days, a.top_fraction, a.judge_top, a.replicates, a.seed)
