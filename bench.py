@@ -414,7 +414,8 @@ def run_batched(args, pt, torch, stream, local):
     sp = ctypes.c_void_p(stream.cuda_stream)
     b = pt.PandemicBatch(params, seeds, stream=sp)
     b.setup()
-    tuning = b.autotune()   # launch shapes for this batch (part of the warm-up)
+    # launch shapes for this batch (part of the warm-up)
+    tuning = b.autotune() if args.tuning == "auto" else b.tuning()
     K, persons, padded = b.size()
     sizes = [b.info(k)["number_people"] for k in range(K)]
     for _ in range(args.batch_warmup):
@@ -466,7 +467,8 @@ def run_batched(args, pt, torch, stream, local):
     e0.record(stream)
     b2 = pt.PandemicBatch(params, seeds, stream=sp)
     b2.setup()
-    b2.autotune()   # the shapes chosen above for this batch size (cached: no timing runs)
+    if args.tuning == "auto":
+        b2.autotune()   # the shapes chosen above for this batch size (cached: no timing runs)
     b2.run()
     b2.final_gen_counts()
     e2e_pd = sum(n * int(d) for n, d in zip(sizes, b2.days_run()))
@@ -665,6 +667,8 @@ def main():
     ap.add_argument("--search-judge", type=int, default=4,
                     help="intervention search at 50M: top-1%% scenarios re-simulated (32 replicates each; 0: skip)")
     ap.add_argument("--only-surrogate", action="store_true", help="run the surrogate section alone")
+    ap.add_argument("--tuning", default="auto", choices=["auto", "default"],
+                    help="launch shapes: chosen by pt_autotune, or the library's defaults (profiling captures)")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="population scale (profiling captures only; the bench line is for 1.0)")
     args = ap.parse_args()
@@ -698,7 +702,8 @@ def main():
     N, L = info["number_people"], info["number_workplaces"]
     Bc_wd = 2 * (L - info["type_offset"][8])
     Bc_we = 10 * (L - info["type_offset"][9])
-    tuning = sim.autotune()   # launch shapes (untimed, before the warm-up)
+    # launch shapes (untimed, before the warm-up)
+    tuning = sim.autotune() if args.tuning == "auto" else sim.tuning()
 
     # warm-up steps (untimed)
     for _ in range(args.warmup):
@@ -793,7 +798,8 @@ def main():
         for _ in range(args.e2e_steps):
             s2 = pt.PandemicSim(params, seed, stream=ctypes.c_void_p(stream.cuda_stream))
             s2.setupSim()
-            s2.autotune()   # the shapes chosen above for this size (cached: no timing runs)
+            if args.tuning == "auto":
+                s2.autotune()   # the shapes chosen above for this size (cached: no timing runs)
             c2, i2 = s2.runToCompletion()
             s2.final_gen_counts()
             e2e_days += len(i2)
