@@ -197,6 +197,8 @@ typedef struct pt_tuning {
                                    of entries the schedule kernel appends: 0 none; 1, 2, 3
                                    when the instance's infected are at least a quarter of,
                                    as many as, twice its buckets */
+    int radix_threads;          /* threads per block of a day's radix passes: 256 (16 entries
+                                   each) or 512 (8 each; radix_blocks_per_sm at most 2) */
 } pt_tuning;
 
 /* Sets / reads the launch shapes of sim (allowed before or after pt_setup). */

@@ -75,7 +75,8 @@ class Interventions(ctypes.Structure):
 class Tuning(ctypes.Structure):
     """Launch shapes of the day's kernels (pt_tuning); every choice gives identical results."""
     _fields_ = [("infect_coop", ctypes.c_int), ("infect_blocks_per_sm", ctypes.c_int),
-                ("radix_blocks_per_sm", ctypes.c_int), ("sched_tf", ctypes.c_int), ("dense_level", ctypes.c_int)]
+                ("radix_blocks_per_sm", ctypes.c_int), ("sched_tf", ctypes.c_int), ("dense_level", ctypes.c_int),
+                ("radix_threads", ctypes.c_int)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -319,8 +319,7 @@ cudaError_t launch_count_keys(const int32_t *keys, int n, int32_t *count, cudaSt
 // pass in ascending person order; each pass ranks a tile of 4096 entries by digit
 // (warp-blocked, so the rank is stable), finds the tile's global position per digit
 // by a decoupled look-back over earlier tiles (one thread per digit), and writes.
-constexpr int kRadixThreads = 256, kRadixWarps = 8, kRadixItems = 16;
-constexpr int kRadixWarpItems = kRadixItems * 32;
+constexpr int kRadixThreads = 256, kRadixItems = 16;   // the default block: 256 threads x 16 entries
 constexpr int kRadixTile = kRadixThreads * kRadixItems;
 static_assert(kRadixTile == kRadixTileEntries, "the host sizes the radix look-back words by kRadixTileEntries");
 
@@ -372,8 +371,8 @@ __device__ __forceinline__ uint32_t pack_rank(unsigned d, unsigned rank, unsigne
 // segments' tiles are numbered consecutively (segment k owns tiles
 // [tile_prefix[k], tile_prefix[k + 1])), and the look-back of a segment's first tile
 // starts from zero.  Unsegmented sorts are one segment [0, E).
-template <int MODE>
-__global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t *__restrict__ keys_in,
+template <int MODE, int THREADS>
+__global__ void __launch_bounds__(THREADS, THREADS == 256 ? 3 : 2) k_radix_pass(const uint32_t *__restrict__ keys_in,
                                                                  const uint32_t *__restrict__ vals_in,
                                                                  uint32_t *__restrict__ keys_out,
                                                                  uint32_t *__restrict__ vals_out, int E_arg,
@@ -383,13 +382,16 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
                                                                  RadixSegments sg, unsigned long long *status,
                                                                  int *ctl, int *error, const int *skip)
 {
+    // a tile of kRadixTile entries: THREADS threads, ITEMS entries each
+    constexpr int WARPS = THREADS / 32, ITEMS = kRadixTile / THREADS, WARP_ITEMS = ITEMS * 32;
+    static_assert(THREADS >= 256 && ITEMS * THREADS == kRadixTile, "one thread per digit and whole tiles");
     if (skip && *(volatile const int *)skip) return;
     __shared__ int s_tile;
     // segment, tile within it, entry base, entry count; for a dense segment of a day's
     // first pass: 1, the instance's persons, first person and first bucket
     __shared__ int s_seg[8];
     __shared__ unsigned s_epoch;
-    __shared__ int s_hist[kRadixWarps][256];
+    __shared__ int s_hist[WARPS][256];
     __shared__ int s_base[256];   // global position of the tile's first entry of each digit
     __shared__ int s_toff[256];   // tile-local position of each digit's first entry
     __shared__ uint32_t s_key[kRadixTile];
@@ -451,11 +453,11 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
         if (tile >= tiles) break;
         const int seg = s_seg[0], stile = s_seg[1], sbase = s_seg[2], scount = s_seg[3];
         const bool dense = s_seg[4] != 0;
-        for (int i = threadIdx.x; i < kRadixWarps * 256; i += kRadixThreads) (&s_hist[0][0])[i] = 0;
+        for (int i = threadIdx.x; i < WARPS * 256; i += THREADS) (&s_hist[0][0])[i] = 0;
         __syncthreads();
-        const int base = stile * kRadixTile + warp * kRadixWarpItems + lane;  // index within the segment
+        const int base = stile * kRadixTile + warp * WARP_ITEMS + lane;  // index within the segment
         const bool full = (stile + 1) * kRadixTile <= scount;
-        uint32_t key[kRadixItems], val[kRadixItems], info[kRadixItems];
+        uint32_t key[ITEMS], val[ITEMS], info[ITEMS];
         if (dense) {
             // the instance's schedule keys, persons implicit (weekday hour-major: entry
             // i < N is person i's hour-0 key, i >= N person i - N's hour-1 key; weekend
@@ -463,7 +465,7 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
             // an unmarked bucket gets the value kDropped and is left out
             const int nk = s_seg[5], pb = s_seg[6], bb = s_seg[7];
 #pragma unroll
-            for (int j = 0; j < kRadixItems; j++) {
+            for (int j = 0; j < ITEMS; j++) {
                 const int i = base + 32 * j;
                 const bool in = full || i < scount;
                 const int kg = in ? sg.day_keys[sbase + i] : bb;
@@ -473,7 +475,7 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
             }
         } else {
 #pragma unroll
-            for (int j = 0; j < kRadixItems; j++) {
+            for (int j = 0; j < ITEMS; j++) {
                 const int i = base + 32 * j;
                 const bool in = full || i < scount;
                 key[j] = in ? keys_in[sbase + i] : 0u;
@@ -487,7 +489,7 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
         }
         // phase A: rank within the warp round, per-warp digit counts
 #pragma unroll
-        for (int j = 0; j < kRadixItems; j++) {
+        for (int j = 0; j < ITEMS; j++) {
             const int i = base + 32 * j;
             bool ok = (full || i < scount) && val[j] != kDropped;
             if ((MODE == kRadixFirst || MODE == kRadixOnly) && mark && ok)
@@ -500,51 +502,53 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
         }
         __syncthreads();
         {
-            // thread d: exclusive bases of the warps for digit d, then the look-back
+            // thread d < 256: exclusive bases of the warps for digit d, then the look-back
             const int d = threadIdx.x;
             int run = 0;
+            if (d < 256) {
 #pragma unroll
-            for (int w = 0; w < kRadixWarps; w++) {
-                int c = s_hist[w][d];
-                s_hist[w][d] = run;
-                run += c;
-            }
-            volatile unsigned long long *st = status;
-            int excl = 0;
-            if (stile == 0) {
-                st[(size_t)tile * 256 + d] = lb_word(epoch, 2, (unsigned)run);
-            } else {
-                st[(size_t)tile * 256 + d] = lb_word(epoch, 1, (unsigned)run);
-                int t = tile - 1;
-                long long spins = 0;
-                while (t >= 0) {
-                    const unsigned long long w = st[(size_t)t * 256 + d];
-                    const unsigned flag = (unsigned)(w >> 32) & 3u;
-                    if ((unsigned)(w >> 34) != epoch || flag == 0) {
-                        if (++spins > kSpinLimit) {
-                            atomicExch(error, 2);
-                            break;
-                        }
-                        __nanosleep(32);
-                        continue;
-                    }
-                    excl += (int)(unsigned)w;
-                    if (flag == 2) break;
-                    t--;
+                for (int w = 0; w < WARPS; w++) {
+                    int c = s_hist[w][d];
+                    s_hist[w][d] = run;
+                    run += c;
                 }
-                st[(size_t)tile * 256 + d] = lb_word(epoch, 2, (unsigned)(excl + run));
+                volatile unsigned long long *st = status;
+                int excl = 0;
+                if (stile == 0) {
+                    st[(size_t)tile * 256 + d] = lb_word(epoch, 2, (unsigned)run);
+                } else {
+                    st[(size_t)tile * 256 + d] = lb_word(epoch, 1, (unsigned)run);
+                    int t = tile - 1;
+                    long long spins = 0;
+                    while (t >= 0) {
+                        const unsigned long long w = st[(size_t)t * 256 + d];
+                        const unsigned flag = (unsigned)(w >> 32) & 3u;
+                        if ((unsigned)(w >> 34) != epoch || flag == 0) {
+                            if (++spins > kSpinLimit) {
+                                atomicExch(error, 2);
+                                break;
+                            }
+                            __nanosleep(32);
+                            continue;
+                        }
+                        excl += (int)(unsigned)w;
+                        if (flag == 2) break;
+                        t--;
+                    }
+                    st[(size_t)tile * 256 + d] = lb_word(epoch, 2, (unsigned)(excl + run));
+                }
+                s_base[d] = sbase + digit_base[((size_t)seg * passes + pass) * 256 + d] + excl;
             }
-            s_base[d] = sbase + digit_base[((size_t)seg * passes + pass) * 256 + d] + excl;
             // tile-local start of digit d (entries of the tile ordered by digit)
             int tile_total;
-            const int toff = block_exclusive_scan<kRadixThreads, int>(run, tile_total);
-            s_toff[d] = toff;
+            const int toff = block_exclusive_scan<THREADS, int>(run, tile_total);
+            if (d < 256) s_toff[d] = toff;
             if (d == 0) s_tile = tile_total;  // reuse: valid entries of this tile
         }
         __syncthreads();
         // phase B: place each entry in shared memory in digit order (stable) ...
 #pragma unroll
-        for (int j = 0; j < kRadixItems; j++) {
+        for (int j = 0; j < ITEMS; j++) {
             const uint32_t r = info[j];
             const bool ok = (r >> 19) & 1u;
             const unsigned d = r & 255u, rank = (r >> 8) & 31u, cnt = (r >> 13) & 63u;
@@ -561,7 +565,7 @@ __global__ void __launch_bounds__(kRadixThreads, 3) k_radix_pass(const uint32_t 
         __syncthreads();
         // ... then write each digit's run with consecutive threads (coalesced)
         const int valid = s_tile;
-        for (int i = threadIdx.x; i < valid; i += kRadixThreads) {
+        for (int i = threadIdx.x; i < valid; i += THREADS) {
             const uint32_t k = s_key[i];
             const unsigned d = (k >> shift) & 255u;
             const int pos = s_base[d] + (i - s_toff[d]);
@@ -596,7 +600,8 @@ cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
     const int P = radix_passes(r.buckets);
     const int bits = key_bits(r.buckets);
     const int tiles = std::max(1, div_up(r.E, kRadixTile));
-    const int bps = std::max(1, std::min(3, r.blocks_per_sm));
+    const bool wide = r.threads == 512;   // 512 threads x 8 entries per tile, at most 2 blocks per SM
+    const int bps = std::max(1, std::min(wide ? 2 : 3, r.blocks_per_sm));
     const int grid = std::max(1, std::min(tiles, bps * sm_count()));  // persistent blocks
     const uint32_t *kin = r.keys;
     const uint32_t *vin = r.vals;   // nullptr: implicit values (entry index -> person)
@@ -615,13 +620,17 @@ cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
 #define PT_RADIX_ARGS kin, vin, kout, vout, r.E, cnt, mk, p, P, nbits, r.N, r.person_mode, r.digit_base, r.seg, r.status, \
                       r.ctl, r.error, r.skip
         if (P == 1 && implicit)
-            k_radix_pass<kRadixOnly><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+            k_radix_pass<kRadixOnly, kRadixThreads><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
         else if (p == 0 && implicit)
-            k_radix_pass<kRadixFirst><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+            k_radix_pass<kRadixFirst, kRadixThreads><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+        else if (p == P - 1 && wide)
+            k_radix_pass<kRadixLast, 512><<<grid, 512, 0, s>>>(PT_RADIX_ARGS);
         else if (p == P - 1)
-            k_radix_pass<kRadixLast><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+            k_radix_pass<kRadixLast, kRadixThreads><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+        else if (wide)
+            k_radix_pass<kRadixMiddle, 512><<<grid, 512, 0, s>>>(PT_RADIX_ARGS);
         else
-            k_radix_pass<kRadixMiddle><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+            k_radix_pass<kRadixMiddle, kRadixThreads><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
 #undef PT_RADIX_ARGS
         count_launch();
         e = cudaGetLastError();
@@ -1454,6 +1463,7 @@ static RadixArgs day_radix_args(const DevArrays &d, bool weekend)
     r.skip = &d.sc->done;
     r.keep_keys = true;  // the bucket offsets come from the sorted keys
     r.blocks_per_sm = d.tune.radix_blocks_per_sm;
+    r.threads = d.tune.radix_threads;
     return r;
 }
 

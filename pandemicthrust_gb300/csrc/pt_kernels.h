@@ -94,6 +94,7 @@ struct Tuning {
                                     // shifts, 1 multiply-add adds, 2 also multiply rotations
     int dense_level = 0;            // when a day's sort reads the schedule keys directly:
                                     // 0 never; 1, 2, 3: infected >= buckets / 4, x 1, x 2
+    int radix_threads = 256;        // threads per block of a day's radix passes: 256 or 512
 };
 
 // Device pointers of a batch of simulations (one simulation is a batch of one).
@@ -212,6 +213,8 @@ struct RadixArgs {
     int *error;
     const int *skip;
     int blocks_per_sm = 3;        // persistent blocks per SM (1..3, the kernel's occupancy bound)
+    int threads = 256;            // threads per block of the explicit-value passes: 256 (16 entries
+                                  // each, up to 3 blocks per SM) or 512 (8 each, up to 2 blocks)
 };
 int radix_passes(int buckets);
 cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s);

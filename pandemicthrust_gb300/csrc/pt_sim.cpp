@@ -840,6 +840,7 @@ static pt_tuning to_public(const ptk::Tuning &t)
     o.radix_blocks_per_sm = t.radix_blocks_per_sm;
     o.sched_tf = t.sched_tf;
     o.dense_level = t.dense_level;
+    o.radix_threads = t.radix_threads;
     return o;
 }
 
@@ -847,7 +848,9 @@ static pt_status engine_set_tuning(Engine *s, const pt_tuning *t)
 {
     if (!t || (t->infect_coop != 0 && t->infect_coop != 1) || t->infect_blocks_per_sm < 1 ||
         t->infect_blocks_per_sm > 32 || t->radix_blocks_per_sm < 1 || t->radix_blocks_per_sm > 3 ||
-        t->sched_tf < 0 || t->sched_tf > 2 || t->dense_level < 0 || t->dense_level > 3)
+        t->sched_tf < 0 || t->sched_tf > 2 || t->dense_level < 0 || t->dense_level > 3 ||
+        (t->radix_threads != 256 && t->radix_threads != 512) ||
+        (t->radix_threads == 512 && t->radix_blocks_per_sm > 2))
         return fail(s, PT_ERR_ARG, "launch shape outside its range");
     ptk::Tuning n;
     n.infect_coop = t->infect_coop;
@@ -855,9 +858,10 @@ static pt_status engine_set_tuning(Engine *s, const pt_tuning *t)
     n.radix_blocks_per_sm = t->radix_blocks_per_sm;
     n.sched_tf = t->sched_tf;
     n.dense_level = t->dense_level;
+    n.radix_threads = t->radix_threads;
     if (n.infect_coop != s->d.tune.infect_coop || n.infect_blocks_per_sm != s->d.tune.infect_blocks_per_sm ||
         n.radix_blocks_per_sm != s->d.tune.radix_blocks_per_sm || n.sched_tf != s->d.tune.sched_tf ||
-        n.dense_level != s->d.tune.dense_level) {
+        n.dense_level != s->d.tune.dense_level || n.radix_threads != s->d.tune.radix_threads) {
         // the captured day loop holds the old launch shapes
         if (s->stream) cudaStreamSynchronize(s->stream);
         if (s->run_graph) cudaGraphExecDestroy(s->run_graph);
@@ -899,7 +903,9 @@ static pt_status engine_autotune(Engine *s, int days, pt_tuning *chosen)
     // thread-per-infector kernel: 9 resident 128-thread blocks per SM at 56 registers;
     // warp-cooperative kernel: 6 resident 256-thread blocks per SM at 40 registers
     const Cand infect[] = {{0, 8}, {0, 4}, {1, 6}, {1, 12}, {1, 3}, {0, 16}};
-    const int radix[] = {3, 2, 1};
+    // radix passes: (blocks per SM, threads per block)
+    const int radix[] = {3, 2, 2};
+    const int radix_threads[] = {256, 256, 512};
     const int tfs[] = {0, 1, 2};
     const int runs = (int)(sizeof(infect) / sizeof(infect[0]));
     float best_inf = 1e30f, best_rad[3] = {1e30f, 1e30f, 1e30f}, best_tf[3] = {1e30f, 1e30f, 1e30f};
@@ -911,6 +917,7 @@ static pt_status engine_autotune(Engine *s, int days, pt_tuning *chosen)
         t.infect_coop = infect[i].coop;
         t.infect_blocks_per_sm = infect[i].bps;
         t.radix_blocks_per_sm = radix[i % 3];
+        t.radix_threads = radix_threads[i % 3];
         t.sched_tf = tfs[(i + 1) % 3];
         t.dense_level = 0;
         pt_status st = engine_set_tuning(s, &t);
@@ -942,6 +949,7 @@ static pt_status engine_autotune(Engine *s, int days, pt_tuning *chosen)
     t.infect_coop = infect[best_i].coop;
     t.infect_blocks_per_sm = infect[best_i].bps;
     t.radix_blocks_per_sm = radix[rbest];
+    t.radix_threads = radix_threads[rbest];
     t.sched_tf = tfs[tbest];
     t.dense_level = 0;
     // the dense-day sort changes both the schedule and the sort stage: its levels are

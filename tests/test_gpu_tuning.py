@@ -14,11 +14,16 @@ from oracle.oracle import Oracle, make_params
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [dict(infect_coop=0, infect_blocks_per_sm=8, radix_blocks_per_sm=3, sched_tf=0, dense_level=0),
-          dict(infect_coop=1, infect_blocks_per_sm=6, radix_blocks_per_sm=2, sched_tf=1, dense_level=1),
-          dict(infect_coop=1, infect_blocks_per_sm=1, radix_blocks_per_sm=1, sched_tf=2, dense_level=2),
-          dict(infect_coop=0, infect_blocks_per_sm=1, radix_blocks_per_sm=1, sched_tf=2, dense_level=3),
-          dict(infect_coop=1, infect_blocks_per_sm=32, radix_blocks_per_sm=3, sched_tf=1, dense_level=1)]
+SHAPES = [dict(infect_coop=0, infect_blocks_per_sm=8, radix_blocks_per_sm=3, sched_tf=0, dense_level=0,
+               radix_threads=256),
+          dict(infect_coop=1, infect_blocks_per_sm=6, radix_blocks_per_sm=2, sched_tf=1, dense_level=1,
+               radix_threads=512),
+          dict(infect_coop=1, infect_blocks_per_sm=1, radix_blocks_per_sm=1, sched_tf=2, dense_level=2,
+               radix_threads=512),
+          dict(infect_coop=0, infect_blocks_per_sm=1, radix_blocks_per_sm=1, sched_tf=2, dense_level=3,
+               radix_threads=256),
+          dict(infect_coop=1, infect_blocks_per_sm=32, radix_blocks_per_sm=3, sched_tf=1, dense_level=1,
+               radix_threads=256)]
 
 FIELDS = ("status_p", "status_s", "day_p", "day_s", "gen_p", "gen_s")
 
@@ -111,11 +116,11 @@ def test_autotune_on_a_plain_simulation_then_run_equals_default(native_lib):
 
 def test_bad_shapes_are_rejected(native_lib):
     sim = pt.PandemicSim(make_params(max_days=2, people_scaling=0.001, location_scaling=0.001), 1)
-    for bad in (dict(infect_coop=2, infect_blocks_per_sm=4, radix_blocks_per_sm=1, sched_tf=0, dense_level=0),
-                dict(infect_coop=0, infect_blocks_per_sm=0, radix_blocks_per_sm=1, sched_tf=0, dense_level=0),
-                dict(infect_coop=0, infect_blocks_per_sm=4, radix_blocks_per_sm=4, sched_tf=0, dense_level=0),
-                dict(infect_coop=0, infect_blocks_per_sm=4, radix_blocks_per_sm=1, sched_tf=3, dense_level=0),
-                dict(infect_coop=0, infect_blocks_per_sm=4, radix_blocks_per_sm=1, sched_tf=0, dense_level=4)):
+    ok = dict(infect_coop=0, infect_blocks_per_sm=4, radix_blocks_per_sm=1, sched_tf=0, dense_level=0,
+              radix_threads=256)
+    for bad in (dict(ok, infect_coop=2), dict(ok, infect_blocks_per_sm=0), dict(ok, radix_blocks_per_sm=4),
+                dict(ok, sched_tf=3), dict(ok, dense_level=4), dict(ok, radix_threads=384),
+                dict(ok, radix_threads=512, radix_blocks_per_sm=3)):
         with pytest.raises(pt.PtError):
             sim.set_tuning(bad)
     sim.close()
