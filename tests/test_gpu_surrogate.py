@@ -163,3 +163,23 @@ def test_ensemble_mean_on_device_matches_the_members(native_lib):
     np.testing.assert_allclose(s.raw_features(X), want, rtol=1e-5, atol=1e-6)
     assert s.raw_features(X[:0]).shape == (0, sg.OUTPUTS)
     s.close()
+
+
+def test_intervention_search_screens_then_judges_with_the_simulator(native_lib):
+    """The surrogate-screened search end to end at a small size: every candidate is
+    scored, the top fraction is kept, its best are re-simulated with replicates, and
+    the simulator's pick is among the judged candidates and within the budget."""
+    import os
+    if not os.path.exists(sg.SHIPPED_MODEL):
+        pytest.skip("no shipped surrogate")
+    s = sg.Surrogate.load(sg.SHIPPED_MODEL, max_batch=4096)
+    r = sg.search(s, persons=300_000, candidates=3000, budget_days=14, top_fraction=0.01, judge_top=2,
+                  replicates=3, transfer_sample=2, seed_base=400_000_000)
+    s.close()
+    assert r["candidates"] == 3000 and r["top"] == 30 and r["judged"] == 2 and r["transfer_sample"] == 2
+    assert r["abm_runs"] == 12 and r["abm_person_days_per_s"] > 0 and r["surrogate_scenarios_per_s"] > 0
+    assert r["abm_choice"]["closure_days"] <= 14 and r["abm_choice"]["vaccination"] == 0.2
+    assert r["seeds_at_persons"] == 6   # 20 per million, scaled to 300,000 persons
+    assert r["error_judged"]["pairs"] == 4
+    # the best candidates by the surrogate hold the epidemic down in the simulator too
+    assert sum(r["abm_choice"]["simulated_attack"]) < 0.2
