@@ -172,8 +172,9 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g)
 // offset) is 128 B and the row-group stride (stride byte offset) is KG * 128 B; the
 // MMA over K columns [16 s, 16 s + 16) starts at +256 s.
 constexpr int kUmmaM = 128;           // rows per tile (the MMA's M)
-constexpr int kUmmaThreads = 256;     // eight warps: warp w reads accumulator lanes 32 (w % 4).. + 31,
-                                      // the 32-column chunks of parity w / 4
+constexpr int kUmmaThreads = 512;     // sixteen warps: warp w reads accumulator lanes 32 (w % 4).. + 31,
+                                      // the 32-column chunks c with c % 4 == w / 4
+constexpr int kUmmaColGroups = kUmmaThreads / 128;
 constexpr int kUmmaMaxN = 256, kUmmaMaxK = 256;
 constexpr int kUmmaSmem = 1024 + (kUmmaMaxN + kUmmaM) * kUmmaMaxK * 2;   // barrier page + B + A
 constexpr long long kUmmaSpin = 1ll << 22;   // polls of the MMA-completion barrier before giving up
@@ -286,10 +287,10 @@ __global__ void __launch_bounds__(kUmmaThreads, 1)
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;");
         // epilogue: warp w reads accumulator lanes (rows) 32 (w % 4) .. + 31, 32 columns at
-        // a time, the chunks of parity w / 4
+        // a time, every kUmmaColGroups-th chunk from chunk w / 4
         const int quarter = warp & 3;
         const int row = m0 + 32 * quarter + lane;
-        for (int c0 = 32 * (warp >> 2); c0 < Np; c0 += 64) {
+        for (int c0 = 32 * (warp >> 2); c0 < Np; c0 += 32 * kUmmaColGroups) {
             uint32_t v[32];
             const uint32_t taddr = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)c0;
             asm volatile(
