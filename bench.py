@@ -851,9 +851,9 @@ def main():
             "tuning": tuning,
             "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "traffic_source": ("DRAM bytes per launch of one ncu capture at 20M persons "
-                                            "(profiles/ncu_schedule_20M.md), scaled by persons to this workload "
-                                            "(profiles/ncu_traffic.txt)") if traffic else None},
+                         "traffic_source": ("mean DRAM bytes per launch over one 100-day run of this workload, "
+                                            "one-pass ncu capture (profiles/ncu_schedule_traffic_50M.md, "
+                                            "profiles/ncu_traffic.txt)") if traffic else None},
             "int_roofline": int_roof(dominant, nwd, nwe),
             "day_roofline": {"achieved": day_achieved, "peak": peak, "unit": "GB/s", "frac": day_achieved / peak,
                              "bytes_per_run": all_bytes},
