@@ -573,7 +573,7 @@ def run_surrogate(args):
     seconds = {"test_data": t_test_sim}
     if os.path.exists(sg.SHIPPED_MODEL):
         import torch
-        s = sg.Surrogate.load(sg.SHIPPED_MODEL, max_batch=65536)   # chunks that fill the SMs
+        s = sg.Surrogate.load(sg.SHIPPED_MODEL, max_batch=262144)   # one chunk: 13.5 row tiles per SM
         pred, _ = s.predict(test)
         # device time of the ensemble's kernels alone (inputs and outputs resident),
         # CUDA events on the networks' stream (the legacy default stream)

@@ -289,11 +289,13 @@ pt_status pt_mlp_predict_ensemble(pt_mlp *const *members, int count, const float
 /* The same with x (n x widths[0]) and y (n x widths[layers]) in device memory: no
  * copies and no synchronisation; the work is queued on the first network's stream. */
 pt_status pt_mlp_predict_ensemble_device(pt_mlp *const *members, int count, const float *x, int n, float *y);
-/* Inference (pt_mlp_predict*) runs on the tcgen05 tensor-core kernel by default (BF16
- * operands in shared memory, FP32 accumulator in tensor memory) when every layer is
- * at most 256 wide and hidden widths are multiples of 32; enabled = 0 selects the
- * warp-level mma.sync kernel that training uses.  Both accumulate in FP32 and round
- * activations to BF16, so they agree to FP32 summation order. */
+/* Inference (pt_mlp_predict*) runs on the tcgen05 tensor-core kernel by default (TMA
+ * operand loads into shared memory, FP32 accumulators in tensor memory) when every
+ * layer is at most 256 wide and hidden widths are multiples of 32; enabled = 0
+ * selects the warp-level mma.sync kernel that training uses.  Both accumulate in FP32
+ * and round activations to BF16.  The tcgen05 epilogue evaluates GELU in a
+ * polynomial-exponential form within 1.5e-7 of the erf form the mma.sync kernel uses,
+ * so the paths agree to FP32 summation order and that difference. */
 pt_status pt_mlp_set_tcgen05(pt_mlp *mlp, int enabled);
 void pt_mlp_destroy(pt_mlp *mlp);
 const char *pt_mlp_last_error(const pt_mlp *mlp);

@@ -11,6 +11,7 @@
 // m16n8k16 (BF16 in, FP32 accumulate): one kernel with strided operands serves the
 // forward product X W^T, the data gradient dZ W and the weight gradient dZ^T X.
 // Inference over large batches runs every layer on tcgen05.mma (k_umma_layer below).
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -158,35 +159,193 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g)
 }
 
 // ---------------------------------------------------------------- tcgen05 inference
-// Forward layers for inference on the fifth-generation tensor cores: tcgen05.mma
-// (kind::f16, BF16 operands, FP32 accumulator in tensor memory), issued by one thread,
-// with both operands K-major in shared memory and the accumulator read back with
-// tcgen05.ld for the bias + GELU epilogue.  One CTA per SM (persistent): it keeps the
-// layer's whole weight matrix (Np x Kp BF16, at most 256 x 256 = 128 KB) in shared
-// memory and walks 128-row tiles of the batch: load the tile (128 x Kp BF16), one
-// MMA per 16 columns of K into a 128 x Np accumulator, epilogue.
+// Forward layers for inference on the fifth-generation tensor cores.  One persistent
+// CTA per SM, in three roles:
+//   warp 0 (one lane), the producer: loads the layer's weights (Np x Kp BF16, at most
+//     256 x 256 = 128 KB) once, then streams 128-row tiles of the input through a ring
+//     of kUmmaStages shared-memory stages (up to 128 K columns each) with TMA
+//     (cp.async.bulk.tensor), each stage completing on its `full` mbarrier;
+//   warp 1 (one lane), the MMA issuer: per tile it waits for a free accumulator (two
+//     128 x 256 FP32 accumulators in tensor memory, all 512 columns), then per stage
+//     waits for `full`, issues tcgen05.mma (kind::f16, K = 16 each) and commits the
+//     stage back to the producer (`empty`); the tile's last commit goes to the
+//     epilogue (`acc_full`);
+//   the epilogue warps: read the accumulator with tcgen05.ld.32x32b (warp w reads
+//     lanes, i.e. tile rows, 32 (w % 4) .. + 31), add the bias, apply GELU, store,
+//     and release the accumulator (`acc_empty`).
+// So the fill of tile i + 1, its MMAs and the epilogue of tile i overlap.  Every wait
+// is bounded: one that gives up sets the error word and a shared flag that ends every
+// role's loop; the MMA issuer then waits (bounded) for its last MMAs and the producer
+// for its last copies before the tensor memory is freed.
 //
-// Shared-memory operand layout (no swizzle, K-major): 8-row x 16-byte core matrices,
-// core (row group g, K group c) at byte (g * KG + c) * 128 with KG = Kp / 8, row r of
-// a core at +16 r.  So the K-direction core stride (the descriptor's leading byte
-// offset) is 128 B and the row-group stride (stride byte offset) is KG * 128 B; the
-// MMA over K columns [16 s, 16 s + 16) starts at +256 s.
-constexpr int kUmmaM = 128;           // rows per tile (the MMA's M)
-constexpr int kUmmaThreads = 512;     // sixteen warps: warp w reads accumulator lanes 32 (w % 4).. + 31,
-                                      // the 32-column chunks c with c % 4 == w / 4
-constexpr int kUmmaColGroups = kUmmaThreads / 128;
+// Shared-memory operand layouts (K-major), each written by TMA boxes as they land:
+//  * 128-byte swizzle, when K is a multiple of 64: a box is 64 columns (128 bytes) x R
+//    rows, row r at byte 128 r of its block with its eight 16-byte pieces permuted by
+//    r % 8 (the TMA's SWIZZLE_128B); blocks of 64 columns follow each other at 128 R
+//    bytes.  Descriptor: stride byte offset 1024 (eight rows), swizzle mode 128-byte;
+//    the MMA over K columns [16 s, 16 s + 16) starts at block s / 4, byte 32 (s % 4).
+//  * no swizzle, otherwise: a box is 8 columns (16 bytes) x R rows, so the 8-row x
+//    16-byte core matrix (row group g, K group c) sits at byte (c R / 8 + g) * 128.
+//    The K-direction core stride (leading byte offset) is 16 R bytes, the row-group
+//    stride (stride byte offset) 128 bytes; the MMA over K columns [16 s, 16 s + 16)
+//    starts at byte 32 R s.
+// Wide boxes matter: a 16-byte box row is one request that moves a 32-byte sector.
+constexpr int kUmmaM = 128;                    // rows per tile (the MMA's M)
+constexpr int kUmmaStages = 3;                 // input stages in the ring
+constexpr int kUmmaKS = 128;                   // K columns per stage at most
 constexpr int kUmmaMaxN = 256, kUmmaMaxK = 256;
-constexpr int kUmmaSmem = 1024 + (kUmmaMaxN + kUmmaM) * kUmmaMaxK * 2;   // barrier page + B + A
-constexpr long long kUmmaSpin = 1ll << 22;   // polls of the MMA-completion barrier before giving up
+constexpr int kUmmaStageBytes = kUmmaM * kUmmaKS * 2;
+constexpr int kUmmaBarBytes = 1024, kUmmaBiasBytes = 4 * kUmmaMaxN;
+constexpr int kUmmaSmem = kUmmaBarBytes + kUmmaBiasBytes + kUmmaMaxN * kUmmaMaxK * 2 + kUmmaStages * kUmmaStageBytes;
+constexpr int kUmmaEpiWarps = 8;               // epilogue warps: two per lane quarter
+constexpr long long kUmmaSpin = 1ll << 22;     // polls of an mbarrier before a wait gives up
+static_assert(kUmmaSmem <= 227 * 1024, "the tcgen05 layer needs more shared memory than a CTA has");
+
+// The epilogue's GELU: max(z, 0) - a 2^p(-a), a = min(|z|, kGeluClamp), p a degree-7
+// polynomial for log2(Phi(-a)) (coefficients of (-a)^k, from fit_gelu.py beside this
+// file).  Equal to z Phi(z) within 1.5e-7 absolute on every z; the exp2 is ex2.approx.
+constexpr float kGelu0 = -9.999998808e-01f, kGelu1 = 1.151111007e+00f, kGelu2 = -4.591529965e-01f,
+                kGelu3 = 5.269147828e-02f, kGelu4 = 7.389675826e-03f, kGelu5 = 4.214611836e-04f,
+                kGelu6 = -5.384269025e-05f, kGelu7 = -8.463827726e-06f;
+constexpr float kGeluClamp = 5.656854153e+00f;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
+// two FP32 lanes in one 64-bit register, for the paired FP32 instructions (f32x2)
+__device__ __forceinline__ uint64_t f2(float lo, float hi)
+{
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+
+__device__ __forceinline__ void f2_split(uint64_t x, float &lo, float &hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(x));
+}
+
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c)
+{
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b)
+{
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// BF16 pair, lo in the low half (round to nearest even)
+__device__ __forceinline__ uint32_t bf16x2(float lo, float hi)
+{
+    uint32_t d;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
+}
+
+// GELU of a pair of pre-activations, packed to BF16
+__device__ __forceinline__ uint32_t gelu_bf16x2(uint64_t z)
+{
+    float z0, z1;
+    f2_split(z, z0, z1);
+    const float n0 = fmaxf(-fabsf(z0), -kGeluClamp), n1 = fmaxf(-fabsf(z1), -kGeluClamp);   // -a
+    const uint64_t n = f2(n0, n1);
+    uint64_t p = f2_fma(f2(kGelu7, kGelu7), n, f2(kGelu6, kGelu6));
+    p = f2_fma(p, n, f2(kGelu5, kGelu5));
+    p = f2_fma(p, n, f2(kGelu4, kGelu4));
+    p = f2_fma(p, n, f2(kGelu3, kGelu3));
+    p = f2_fma(p, n, f2(kGelu2, kGelu2));
+    p = f2_fma(p, n, f2(kGelu1, kGelu1));
+    p = f2_fma(p, n, f2(kGelu0, kGelu0));
+    float p0, p1;
+    f2_split(p, p0, p1);
+    float r0, r1;
+    f2_split(f2_fma(n, f2(ex2_approx(p0), ex2_approx(p1)), f2(fmaxf(z0, 0.f), fmaxf(z1, 0.f))), r0, r1);
+    return bf16x2(r0, r1);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Waits for the phase of the given parity to complete; false when it gives up after
+// kUmmaSpin polls or when another role has raised `fail` (if given).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, const volatile int *fail)
+{
+    for (long long i = 0; i < kUmmaSpin; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (fail && (i & 63) == 63 && *fail) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void umma_fail(volatile int *fail, int *error)
+{
+    *fail = 1;
+    atomicExch(error, 1);
+}
+
+// TMA: the box at element coordinates (x, y) of the map into shared memory at dst,
+// completing on the mbarrier
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d, uint64_t ad, uint64_t bd, uint32_t idesc, bool accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(ad), "l"(bd), "r"(idesc), "r"((uint32_t)accumulate));
+}
+
+// the mbarrier completes when every tcgen05.mma this thread issued before has completed
+__device__ __forceinline__ void umma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
 // tcgen05 shared-memory matrix descriptor: start >> 4 (bits 0-13), leading byte offset
-// >> 4 (16-29), stride byte offset >> 4 (32-45), the fixed 0b001 (46-48), no swizzle.
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+// >> 4 (16-29), stride byte offset >> 4 (32-45), the fixed 0b001 (46-48), base offset 0
+// (49-51, the operands are 1024-byte aligned), the swizzle mode (61-63: 0 none,
+// 2 128-byte).
+constexpr uint32_t kSwizzleNone = 0, kSwizzle128B = 2;
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo, uint32_t swizzle)
 {
     return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
-           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46) | ((uint64_t)swizzle << 61);
 }
 
 // Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and B
@@ -196,148 +355,268 @@ __host__ __device__ constexpr uint32_t umma_idesc(int M, int N)
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// Copies rows [r0, r0 + R) x Kp BF16 (row stride ld elements) into the core-matrix
-// layout at dst with asynchronous 16-byte copies (every thread issues all of its
-// copies before waiting, so the whole tile is in flight at once); rows at or past
-// `rows` are zero-filled.  The caller waits with umma_fill_wait.
-__device__ __forceinline__ void umma_fill(uint8_t *dst, const bf16 *src, long long ld, int r0, int R, int rows, int Kp)
+// tcgen05.ld of 32 consecutive accumulator columns of the warp's 32 lanes (one row a
+// thread).  The registers are written asynchronously: read them only after
+// tmem_ld_wait on the same array.
+__device__ __forceinline__ void tmem_ld32_issue(uint32_t taddr, uint32_t v[32])
 {
-    const int KG = Kp / 8, chunks = R * KG;
-    for (int q = threadIdx.x; q < chunks; q += blockDim.x) {
-        const int r = q / KG, c = q % KG;
-        const bool in = r0 + r < rows;
-        const bf16 *g = in ? src + (long long)(r0 + r) * ld + 8 * c : src;
-        const uint32_t s = smem_u32(dst + ((r >> 3) * KG + c) * 128 + (r & 7) * 16);
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(s), "l"(g), "r"(in ? 16 : 0) : "memory");
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
 }
 
-__device__ __forceinline__ void umma_fill_wait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
-// One layer: out = act(A W^T + bias) over M rows.  A: M x Kp BF16 (row stride lda);
-// W: Np x Kp BF16 (zero rows past N); Kp a multiple of 16, Np of 16, both <= 256.
-// Hidden layers (H set) store BF16 activations (row stride ldh); the last layer
-// (Z set) stores FP32 outputs (row stride N).  error: set when a wait gives up.
-__global__ void __launch_bounds__(kUmmaThreads, 1)
-    k_umma_layer(const bf16 *A, long long lda, int M, int Kp, const bf16 *W, int Np, int N, const float *bias, int gelu,
-                 bf16 *H, long long ldh, float *Z, int *error)
+// Waits for the warp's tcgen05.ld; the array is an operand so that no use of it is
+// moved above the wait.
+__device__ __forceinline__ void tmem_ld_wait(uint32_t v[32])
 {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7]),
+                   "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]), "+r"(v[12]), "+r"(v[13]), "+r"(v[14]),
+                   "+r"(v[15]), "+r"(v[16]), "+r"(v[17]), "+r"(v[18]), "+r"(v[19]), "+r"(v[20]), "+r"(v[21]),
+                   "+r"(v[22]), "+r"(v[23]), "+r"(v[24]), "+r"(v[25]), "+r"(v[26]), "+r"(v[27]), "+r"(v[28]),
+                   "+r"(v[29]), "+r"(v[30]), "+r"(v[31])
+                 :
+                 : "memory");
+}
+
+// The epilogue of one 32-column chunk of a tile row (v: its accumulator values): bias,
+// GELU and BF16 stores for hidden layers (H), the accumulating FP32 stores for the last.
+__device__ __forceinline__ void epilogue_chunk(const uint32_t v[32], int c0, long long row, const float *s_bias,
+                                               int N, int gelu, bf16 *H, long long ldh, float *Y, long long ldy,
+                                               float scale, int first, int vec)
+{
+    if (H) {
+        const float4 *bq = reinterpret_cast<const float4 *>(s_bias + c0);
+        uint32_t packed[16];
+#pragma unroll
+        for (int j = 0; j < 32; j += 4) {
+            const float4 bb = bq[j / 4];
+            const uint64_t z01 = f2_add(f2(__uint_as_float(v[j]), __uint_as_float(v[j + 1])), f2(bb.x, bb.y));
+            const uint64_t z23 = f2_add(f2(__uint_as_float(v[j + 2]), __uint_as_float(v[j + 3])), f2(bb.z, bb.w));
+            if (gelu) {
+                packed[j / 2] = gelu_bf16x2(z01);
+                packed[j / 2 + 1] = gelu_bf16x2(z23);
+            } else {
+                float a0, a1, a2, a3;
+                f2_split(z01, a0, a1);
+                f2_split(z23, a2, a3);
+                packed[j / 2] = bf16x2(a0, a1);
+                packed[j / 2 + 1] = bf16x2(a2, a3);
+            }
+        }
+        // N is a multiple of 32 for hidden layers: two 32-byte stores, whole sectors
+        bf16 *dst = H + row * ldh + c0;
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+            asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(dst + 16 * k),
+                         "r"(packed[8 * k]), "r"(packed[8 * k + 1]), "r"(packed[8 * k + 2]), "r"(packed[8 * k + 3]),
+                         "r"(packed[8 * k + 4]), "r"(packed[8 * k + 5]), "r"(packed[8 * k + 6]),
+                         "r"(packed[8 * k + 7])
+                         : "memory");
+        return;
+    }
+    float *dst = Y + row * ldy + c0;
+    if (vec) {
+        // the four 32-byte runs of the accumulator are loaded together
+        float o[32];
+        if (!first)
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                asm volatile("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                             : "=f"(o[8 * k]), "=f"(o[8 * k + 1]), "=f"(o[8 * k + 2]), "=f"(o[8 * k + 3]),
+                               "=f"(o[8 * k + 4]), "=f"(o[8 * k + 5]), "=f"(o[8 * k + 6]), "=f"(o[8 * k + 7])
+                             : "l"(dst + 8 * k));
+#pragma unroll
+        for (int i = 0; i < 32; i++) {
+            const float z = __uint_as_float(v[i]) + s_bias[c0 + i];
+            o[i] = first ? scale * z : fmaf(scale, z, o[i]);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(dst + 8 * k),
+                         "f"(o[8 * k]), "f"(o[8 * k + 1]), "f"(o[8 * k + 2]), "f"(o[8 * k + 3]), "f"(o[8 * k + 4]),
+                         "f"(o[8 * k + 5]), "f"(o[8 * k + 6]), "f"(o[8 * k + 7])
+                         : "memory");
+    } else {
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            const int c = c0 + j;
+            if (c < N) {
+                const float z = __uint_as_float(v[j]) + s_bias[c];
+                dst[j] = first ? scale * z : fmaf(scale, z, dst[j]);
+            }
+        }
+    }
+}
+
+// One layer: out = act(A W^T + bias) over M rows, EPI epilogue warps.  tmA: the input
+// (M x Kp BF16), box bw x kUmmaM; tmW: the weights (Np x Kp BF16, zero rows past N),
+// box bw x Np; bw = 64 with the 128-byte swizzle (sw, Kp a multiple of 64), else 8.
+// Kp a multiple of 16, Np of 16, both <= 256.  Hidden layers (H set) store
+// BF16 activations (row stride ldh, N a multiple of 32).  The last layer (Y set)
+// accumulates its FP32 outputs z: Y = scale z (first) or Y + scale z, row stride ldy;
+// with `vec` (ldy a multiple of 32, Y 32-byte aligned) in whole 32-byte sectors,
+// columns from N to the next multiple of 32 included (padding).  error: set when a
+// wait gives up.
+template <int EPI>
+__global__ void __launch_bounds__(32 * (2 + EPI), 1)
+    k_umma_layer(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmW, int M, int Kp,
+                 int Np, int N, int sw, const float *bias, int gelu, bf16 *H, long long ldh, float *Y, long long ldy,
+                 float scale, int first, int vec, int *error)
+{
+    static_assert(EPI % 4 == 0, "each of the four lane quarters needs the same number of epilogue warps");
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + 64);
-    uint8_t *sB = smem + 1024;
-    uint8_t *sA = sB + (size_t)Np * Kp * 2;
+    // barrier page: full[S], empty[S], acc_full[2], acc_empty[2], weights, drain;
+    // then the tensor-memory address and the failure flag
+    const uint32_t b_full = smem_u32(smem), b_empty = b_full + 8 * kUmmaStages, b_accf = b_empty + 8 * kUmmaStages,
+                   b_acce = b_accf + 16, b_w = b_acce + 16, b_drain = b_w + 8;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + 256);
+    volatile int *fail = reinterpret_cast<volatile int *>(smem + 320);
+    float *s_bias = reinterpret_cast<float *>(smem + kUmmaBarBytes);
+    uint8_t *sW = smem + kUmmaBarBytes + kUmmaBiasBytes;
+    const uint32_t sW_u = smem_u32(sW), sA_u = sW_u + kUmmaMaxN * kUmmaMaxK * 2;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tmem_slot)));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
+    if (threadIdx.x == 32) {
+        for (int i = 0; i < kUmmaStages; i++) {
+            mbar_init(b_full + 8 * i, 1);
+            mbar_init(b_empty + 8 * i, 1);
+        }
+        for (int i = 0; i < 2; i++) {
+            mbar_init(b_accf + 8 * i, 1);
+            mbar_init(b_acce + 8 * i, EPI);
+        }
+        mbar_init(b_w, 1);
+        mbar_init(b_drain, 1);
+        *fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
-    umma_fill(sB, W, Kp, 0, Np, Np, Kp);   // waited for with the first tile's fill
+    for (int c = threadIdx.x; c < kUmmaMaxN; c += blockDim.x) s_bias[c] = c < N ? bias[c] : 0.f;
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = *tmem_slot;
-    const uint32_t KG = (uint32_t)Kp / 8;
-    const uint32_t idesc = umma_idesc(kUmmaM, Np);
     const int tiles = (M + kUmmaM - 1) / kUmmaM;
-    uint32_t phase = 0;
-    bool failed = false;
-    for (int t = blockIdx.x; t < tiles && !failed; t += gridDim.x) {
-        const int m0 = t * kUmmaM;
-        umma_fill(sA, A, lda, m0, kUmmaM, M, Kp);
-        umma_fill_wait();
-        asm volatile("fence.proxy.async.shared::cta;");
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        if (threadIdx.x == 0) {
-            const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
-            for (int s = 0; s < Kp / 16; s++) {
-                const uint64_t ad = umma_desc(a0 + 256u * s, 128u, KG * 128u);
-                const uint64_t bd = umma_desc(b0 + 256u * s, 128u, KG * 128u);
-                const uint32_t acc = s > 0 ? 1u : 0u;
-                asm volatile(
-                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                smem_u32(bar)));
-        }
-        // wait for the MMAs (bounded; the outcome is made uniform over the block)
-        long long spins = 0;
-        uint32_t done = 0;
-        while (!done) {
-            asm volatile(
-                "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-                : "=r"(done)
-                : "r"(smem_u32(bar)), "r"(phase));
-            if (!done && ++spins > kUmmaSpin) break;
-        }
-        if (__syncthreads_or(!done)) {
-            if (threadIdx.x == 0) atomicExch(error, 1);
-            failed = true;
-            break;
-        }
-        phase ^= 1u;
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        // epilogue: warp w reads accumulator lanes (rows) 32 (w % 4) .. + 31, 32 columns at
-        // a time, every kUmmaColGroups-th chunk from chunk w / 4
-        const int quarter = warp & 3;
-        const int row = m0 + 32 * quarter + lane;
-        for (int c0 = 32 * (warp >> 2); c0 < Np; c0 += 32 * kUmmaColGroups) {
-            uint32_t v[32];
-            const uint32_t taddr = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)c0;
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-                "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
-                  "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
-                  "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
-                  "=r"(v[30]), "=r"(v[31])
-                : "r"(taddr));
-            asm volatile("tcgen05.wait::ld.sync.aligned;");
-            if (row >= M) continue;
-            if (H) {
-                uint32_t packed[16];
-#pragma unroll
-                for (int j = 0; j < 32; j += 2) {
-                    const int c = c0 + j;
-                    float z0 = __uint_as_float(v[j]) + (c < N ? bias[c] : 0.f);
-                    float z1 = __uint_as_float(v[j + 1]) + (c + 1 < N ? bias[c + 1] : 0.f);
-                    if (gelu) {
-                        z0 = 0.5f * z0 * (1.f + erff(z0 * 0.70710678118654752f));
-                        z1 = 0.5f * z1 * (1.f + erff(z1 * 0.70710678118654752f));
+    const int bw = sw ? 64 : 8;   // K columns per TMA box
+    // K columns per stage: all of K up to kUmmaKS, else about half, in whole boxes and MMA steps
+    const int KS = Kp <= kUmmaKS ? Kp : (sw ? 64 * ((Kp / 64 + 1) / 2) : 16 * ((Kp / 16 + 1) / 2));
+    const int nks = (Kp + KS - 1) / KS;                              // stages per tile: 1 or 2
+    if (warp == 0) {
+        if (lane == 0) {
+            // producer
+            mbar_expect_tx(b_w, (uint32_t)(Np * Kp * 2));
+            for (int c = 0; c < Kp / bw; c++) tma_load_2d(sW_u + c * Np * bw * 2, &tmW, bw * c, 0, b_w);
+            bool ok = true;
+            int it = 0;   // stage fills issued
+            for (int t = blockIdx.x; ok && t < tiles; t += gridDim.x)
+                for (int ks = 0; ks < nks; ks++) {
+                    const int s = it % kUmmaStages, use = it / kUmmaStages;
+                    if (use > 0 && !mbar_wait(b_empty + 8 * s, (use - 1) & 1, fail)) {
+                        ok = false;
+                        break;
                     }
-                    packed[j / 2] = pack2(__float2bfloat16(z0), __float2bfloat16(z1));
+                    const int k0 = ks * KS, kc = min(KS, Kp - k0);
+                    const uint32_t dst = sA_u + s * kUmmaStageBytes;
+                    mbar_expect_tx(b_full + 8 * s, (uint32_t)(kUmmaM * kc * 2));
+                    for (int c = 0; c < kc / bw; c++)
+                        tma_load_2d(dst + c * kUmmaM * bw * 2, &tmA, k0 + bw * c, t * kUmmaM, b_full + 8 * s);
+                    it++;
                 }
-                // N is a multiple of 32 for hidden layers: whole 64-byte runs
-                uint4 *dst = reinterpret_cast<uint4 *>(H + (long long)row * ldh + c0);
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    dst[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
-            } else {
-                float *dst = Z + (long long)row * N;
-#pragma unroll
-                for (int j = 0; j < 32; j++) {
-                    const int c = c0 + j;
-                    if (c < N) dst[c] = __uint_as_float(v[j]) + bias[c];
-                }
+            if (!ok) umma_fail(fail, error);
+            // every copy lands before the CTA ends: the last fill of each stage, the weights
+            for (int s = 0; s < kUmmaStages; s++) {
+                const int uses = it / kUmmaStages + (s < it % kUmmaStages ? 1 : 0);
+                if (uses > 0) mbar_wait(b_full + 8 * s, (uses - 1) & 1, nullptr);
             }
+            mbar_wait(b_w, 0, nullptr);
         }
-        // the next tile's MMA overwrites the accumulator and its fill the A operand
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;");
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // MMA issuer
+            bool ok = mbar_wait(b_w, 0, fail);
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t idesc = umma_idesc(kUmmaM, Np);
+            int it = 0, tc = 0;
+            for (int t = blockIdx.x; ok && t < tiles; t += gridDim.x, tc++) {
+                const int b = tc & 1, use = tc >> 1;
+                if (use > 0 && !mbar_wait(b_acce + 8 * b, (use - 1) & 1, fail)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t d = tmem + 256u * b;
+                for (int ks = 0; ks < nks; ks++, it++) {
+                    const int s = it % kUmmaStages, u = it / kUmmaStages;
+                    if (!mbar_wait(b_full + 8 * s, u & 1, fail)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const int k0 = ks * KS, kc = min(KS, Kp - k0);
+                    const uint32_t a0 = sA_u + s * kUmmaStageBytes;
+                    for (int j = 0; j < kc / 16; j++) {
+                        const int g = k0 / 16 + j;   // the MMA step within K
+                        uint64_t ad, wd;
+                        if (sw) {
+                            ad = umma_desc(a0 + (j >> 2) * kUmmaM * 128 + 32 * (j & 3), 16, 1024, kSwizzle128B);
+                            wd = umma_desc(sW_u + (g >> 2) * Np * 128 + 32 * (g & 3), 16, 1024, kSwizzle128B);
+                        } else {
+                            ad = umma_desc(a0 + j * 32 * kUmmaM, 16 * kUmmaM, 128, kSwizzleNone);
+                            wd = umma_desc(sW_u + g * 32 * Np, 16 * Np, 128, kSwizzleNone);
+                        }
+                        umma_bf16(d, ad, wd, idesc, (ks | j) != 0);
+                    }
+                    umma_commit(b_empty + 8 * s);   // the stage is free once these MMAs complete
+                }
+                if (!ok) break;
+                umma_commit(b_accf + 8 * b);
+            }
+            if (!ok) umma_fail(fail, error);
+            // every MMA issued completes before the tensor memory is freed
+            umma_commit(b_drain);
+            mbar_wait(b_drain, 0, nullptr);
+        }
+        __syncwarp();
+    } else {
+        // epilogue: lanes (tile rows) 32 q .. 32 q + 31, 32-column chunks part, part + EPI / 4, ...
+        const int q = warp & 3, part = (warp - 2) >> 2;
+        constexpr int parts = EPI / 4;
+        int tc = 0;
+        for (int t = blockIdx.x; t < tiles; t += gridDim.x, tc++) {
+            const int b = tc & 1, use = tc >> 1;
+            if (!__all_sync(0xffffffffu, mbar_wait(b_accf + 8 * b, use & 1, fail))) {
+                if (lane == 0) umma_fail(fail, error);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const int row = t * kUmmaM + 32 * q + lane;
+            const uint32_t tb = tmem + ((uint32_t)(32 * q) << 16) + 256u * b;
+            for (int c0 = 32 * part; c0 < Np; c0 += 32 * parts) {
+                uint32_t v[32];
+                __syncwarp();   // tcgen05.ld and its wait are warp-collective
+                tmem_ld32_issue(tb + c0, v);
+                tmem_ld_wait(v);
+                if (row < M) epilogue_chunk(v, c0, row, s_bias, N, gelu, H, ldh, Y, ldy, scale, first, vec);
+            }
+            // the accumulator is free for the tile after next
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(b_acce + 8 * b);
+        }
     }
+    asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
 }
 
 // Zero-padded BF16 copies for the tcgen05 path: src rows x cols (row stride cols) ->
@@ -348,6 +627,38 @@ __global__ void k_pad_bf16(const bf16 *src, int rows, int cols, bf16 *dst, int p
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const int r = (int)(i / pcol), c = (int)(i % pcol);
         dst[i] = (r < rows && c < cols) ? src[(long long)r * cols + c] : __float2bfloat16(0.f);
+    }
+}
+
+// The tcgen05 path's input: rows x din FP32 -> rows x kp BF16 (round to nearest even,
+// zero columns past din), one 16-byte group of eight columns per thread.
+__global__ void k_input_bf16(const float *x, int rows, int din, bf16 *dst, int kp)
+{
+    const int groups = kp / 8;
+    const long long n = (long long)rows * groups;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long r = i / groups;
+        const int c0 = (int)(i % groups) * 8;
+        const float *xr = x + r * din;
+        uint32_t w[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int c = c0 + 2 * k;
+            w[k] = bf16x2(c < din ? xr[c] : 0.f, c + 1 < din ? xr[c + 1] : 0.f);
+        }
+        *reinterpret_cast<uint4 *>(dst + r * kp + c0) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
+
+// rows x cols FP32 from src (row stride lds) to dst (contiguous rows), a warp per row
+__global__ void k_compact_rows(const float *src, long long lds, float *dst, int rows, int cols)
+{
+    const int lane = threadIdx.x & 31, wpb = blockDim.x / 32;
+    const long long warps = (long long)gridDim.x * wpb;
+    for (long long r = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); r < rows; r += warps) {
+        const float *s = src + r * lds;
+        float *d = dst + r * cols;
+        for (int c = lane; c < cols; c += 32) d[c] = s[c];
     }
 }
 
@@ -363,11 +674,16 @@ __global__ void k_gather(const float *X, const float *Y, const int *idx, int B, 
         for (int c = threadIdx.x; c < dout; c += blockDim.x) Yb[(long long)row * dout + c] = Y[src * dout + c];
 }
 
-// acc = (first ? 0 : acc) + scale * z over n values
-__global__ void k_accumulate(float *acc, const float *z, long long n, float scale, int first)
+// acc = scale z (first) or acc + scale z over rows x cols (row strides lda, cols), the
+// arithmetic of the tcgen05 layer's accumulating epilogue
+__global__ void k_accumulate(float *acc, long long lda, const float *z, int rows, int cols, float scale, int first)
 {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        acc[i] = first ? scale * z[i] : acc[i] + scale * z[i];
+    const long long n = (long long)rows * cols;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        float *a = acc + (i / cols) * lda + i % cols;
+        *a = first ? scale * z[i] : fmaf(scale, z[i], *a);
+    }
 }
 
 // mean squared error over B x dout; gradient of the output layer
@@ -452,6 +768,9 @@ struct pt_mlp {
     std::vector<int> kpad, npad;
     bf16 *h0p = nullptr;
     int *umma_err = nullptr;
+    // inference output: the last layer's outputs, rows padded to a multiple of 32
+    float *zout = nullptr;
+    int ldz = 0;
 };
 
 static pt_status mfail(pt_mlp *m, pt_status st, const std::string &msg)
@@ -588,15 +907,90 @@ static int sm_count_mlp()
     return n;
 }
 
-// forward pass for inference over the B rows in H[0]: tcgen05 layers when the shapes
-// fit (Z[L-1] receives the outputs, hidden H[l] the activations), else forward().
-static cudaError_t forward_infer(pt_mlp *m, int B)
+// The driver's tensor-map encoder, through the runtime's entry-point query (no link
+// against the driver library).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled()
 {
-    if (!m->use_umma || !umma_fits(m)) return forward(m, B);
+    static const EncodeTiledFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return (EncodeTiledFn) nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// A map over a rows x cols BF16 matrix (row stride ld elements, a multiple of 8) whose
+// box is box_rows rows by 64 columns with the 128-byte swizzle (sw; cols a multiple of
+// 64) or by 8 columns without: the TMA boxes of a tcgen05 operand in the kernel's two
+// shared-memory layouts.  Rows past `rows` read as zeros.
+static bool operand_map(CUtensorMap *map, const bf16 *base, int rows, int cols, long long ld, int box_rows, bool sw)
+{
+    const EncodeTiledFn fn = encode_tiled();
+    if (!fn || ld % 8 != 0 || cols % (sw ? 64 : 8) != 0) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {sw ? 64u : 8u, (cuuint32_t)box_rows};
+    const cuuint32_t elem[2] = {1u, 1u};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16 *>(base), dims, strides, box, elem,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, sw ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+static int pad32(int x) { return (x + 31) / 32 * 32; }
+
+// rows x cols outputs from the padded accumulator (row stride lds) to dst (contiguous
+// rows): on the device straight into dst, for the host through the contiguous device
+// buffer `staging` and one copy.
+static cudaError_t copy_out(const float *src, int lds, float *staging, int rows, int cols, float *dst,
+                            cudaMemcpyKind kind, cudaStream_t s)
+{
+    if (rows == 0) return cudaSuccess;
+    float *to = kind == cudaMemcpyDeviceToDevice ? dst : staging;
+    k_compact_rows<<<std::min((rows + 7) / 8, 8192), 256, 0, s>>>(src, lds, to, rows, cols);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && kind != cudaMemcpyDeviceToDevice)
+        e = cudaMemcpyAsync(dst, staging, (size_t)rows * cols * sizeof(float), kind, s);
+    return e;
+}
+
+// The padded inference output buffer of a network (max_batch x ldz).
+static cudaError_t ensure_zout(pt_mlp *m)
+{
+    if (m->zout) return cudaSuccess;
+    m->ldz = pad32(m->width[m->L]);
+    return dalloc(m, &m->zout, (size_t)m->max_batch * m->ldz);
+}
+
+// forward pass for inference over B rows of x (device, B x width[0] FP32), its outputs
+// z accumulated into y (row stride ldy): y = scale z when `first`, else y + scale z.
+// tcgen05 layers when the shapes fit (hidden H[l] receive the activations, the last
+// layer accumulates in its epilogue), else forward() and k_accumulate.  *x0 caches the
+// zero-padded BF16 copy of x that the tcgen05 layers read: the first network of an
+// ensemble makes it (into its h0p), the others reuse it.
+static cudaError_t forward_infer(pt_mlp *m, int B, const float *x, const bf16 **x0, float *y, long long ldy,
+                                 float scale, bool first)
+{
+    if (!m->use_umma || !umma_fits(m)) {
+        k_gather<<<B, 128, 0, m->stream>>>(x, nullptr, nullptr, B, m->width[0], m->width[m->L], m->H[0], nullptr);
+        cudaError_t e = forward(m, B);
+        if (e != cudaSuccess || B == 0) return e;
+        const long long total = (long long)B * m->width[m->L];
+        k_accumulate<<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, m->stream>>>(
+            y, ldy, m->Z[m->L - 1], B, m->width[m->L], scale, first ? 1 : 0);
+        return cudaGetLastError();
+    }
     cudaError_t e = cudaSuccess;
     if (m->wpk.empty()) {
-        static const cudaError_t attr =
-            cudaFuncSetAttribute(k_umma_layer, cudaFuncAttributeMaxDynamicSharedMemorySize, kUmmaSmem);
+        static const cudaError_t attr = cudaFuncSetAttribute(
+            k_umma_layer<kUmmaEpiWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUmmaSmem);
         if (attr != cudaSuccess) return attr;
         for (int l = 0; l < m->L; l++) {
             m->kpad.push_back(pad16(m->width[l]));
@@ -618,22 +1012,35 @@ static cudaError_t forward_infer(pt_mlp *m, int B)
                 m->wb + m->woff[l], m->width[l + 1], m->width[l], m->wpk[l], m->npad[l], m->kpad[l]);
         m->packed_stale = false;
     }
-    k_pad_bf16<<<grid_for((long long)B * m->kpad[0]), 256, 0, m->stream>>>(m->H[0], B, m->width[0], m->h0p, B,
-                                                                           m->kpad[0]);
+    if (!*x0) {
+        k_input_bf16<<<grid_for((long long)B * m->kpad[0] / 8), 256, 0, m->stream>>>(x, B, m->width[0], m->h0p,
+                                                                                    m->kpad[0]);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        *x0 = m->h0p;
+    }
     const int tiles = (B + kUmmaM - 1) / kUmmaM;
     for (int l = 0; l < m->L; l++) {
         const int Kp = m->kpad[l], Np = m->npad[l];
         const bool last = l + 1 == m->L;
-        // at least 80 KB per CTA: two CTAs per SM at most, within the 512 TMEM columns
-        const int smem = std::max(1024 + (Np + kUmmaM) * Kp * 2, 80 * 1024);
-        const int per_sm = smem > 114 * 1024 ? 1 : 2;
-        const int grid = std::max(1, std::min(tiles, per_sm * sm_count_mlp()));
-        const bf16 *A = l == 0 ? m->h0p : m->H[l];
+        // one CTA per SM: the full shared-memory request keeps a second one off the SM,
+        // so the 512 tensor-memory columns a CTA allocates are always free
+        const int grid = std::max(1, std::min(tiles, sm_count_mlp()));
+        const bf16 *A = l == 0 ? *x0 : m->H[l];
         const long long lda = l == 0 ? m->kpad[0] : m->width[l];
-        k_umma_layer<<<grid, kUmmaThreads, smem, m->stream>>>(A, lda, B, Kp, m->wpk[l], Np, m->width[l + 1],
-                                                             m->w + m->boff[l], last ? 0 : 1,
-                                                             last ? nullptr : m->H[l + 1], m->width[l + 1],
-                                                             last ? m->Z[l] : nullptr, m->umma_err);
+        const bool sw = Kp % 64 == 0;   // the 128-byte swizzled layout: whole 128-byte box rows
+        CUtensorMap ma, mw;
+        if (!operand_map(&ma, A, B, Kp, lda, kUmmaM, sw) || !operand_map(&mw, m->wpk[l], Np, Kp, Kp, Np, sw))
+            return cudaErrorNotSupported;
+        const int N = m->width[l + 1];
+        const float *bias = m->w + m->boff[l];
+        bf16 *Hn = last ? nullptr : m->H[l + 1];
+        float *Yn = last ? y : nullptr;
+        // whole-sector accumulation: 32-column runs fit the row and start 32-byte aligned
+        const int vec = last && ldy % 32 == 0 && ldy >= pad32(N) && reinterpret_cast<uintptr_t>(y) % 32 == 0;
+        k_umma_layer<kUmmaEpiWarps><<<grid, 32 * (2 + kUmmaEpiWarps), kUmmaSmem, m->stream>>>(
+            ma, mw, B, Kp, Np, N, sw ? 1 : 0, bias, last ? 0 : 1, Hn, N, Yn, ldy, scale, first ? 1 : 0, vec,
+            m->umma_err);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
@@ -836,6 +1243,7 @@ pt_status pt_mlp_predict(pt_mlp *m, const float *X, int n, float *Y)
     const int din = m->width[0], dout = m->width[m->L];
     float *dX = nullptr;
     const int chunk = m->max_batch;
+    MCK(ensure_zout(m), "inference output");
     MCK(cudaMalloc(&dX, (size_t)std::max(1, std::min(n, chunk)) * din * sizeof(float)), "batch");
     cudaError_t e = cudaSuccess;
     for (int s0 = 0; s0 < n && e == cudaSuccess; s0 += chunk) {
@@ -843,11 +1251,11 @@ pt_status pt_mlp_predict(pt_mlp *m, const float *X, int n, float *Y)
         e = cudaMemcpyAsync(dX, X + (size_t)s0 * din, (size_t)B * din * sizeof(float), cudaMemcpyHostToDevice,
                             m->stream);
         if (e != cudaSuccess) break;
-        k_gather<<<B, 128, 0, m->stream>>>(dX, nullptr, nullptr, B, din, dout, m->H[0], nullptr);
-        e = forward_infer(m, B);
+        const bf16 *x0 = nullptr;
+        e = forward_infer(m, B, dX, &x0, m->zout, m->ldz, 1.0f, true);
         if (e != cudaSuccess) break;
-        e = cudaMemcpyAsync(Y + (size_t)s0 * dout, m->Z[m->L - 1], (size_t)B * dout * sizeof(float),
-                            cudaMemcpyDeviceToHost, m->stream);
+        e = copy_out(m->zout, m->ldz, m->Z[m->L - 1], B, dout, Y + (size_t)s0 * dout, cudaMemcpyDeviceToHost,
+                     m->stream);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
     cudaFree(dX);
@@ -881,34 +1289,28 @@ pt_status pt_mlp_predict_ensemble(pt_mlp *const *members, int count, const float
     // every member runs on the first member's stream: finish what is queued on its own
     for (int j = 1; j < count; j++)
         if (members[j]->stream != s) MCK(cudaStreamSynchronize(members[j]->stream), "ensemble member stream");
-    float *dX = nullptr, *acc = nullptr;
+    // the members' mean accumulates in the first member's padded output buffer
+    MCK(ensure_zout(m), "inference output");
+    float *dX = nullptr, *acc = m->zout;
     const size_t rows = (size_t)std::max(1, std::min(n, chunk));
     MCK(cudaMalloc(&dX, rows * din * sizeof(float)), "batch");
-    cudaError_t e = cudaMalloc(&acc, rows * dout * sizeof(float));
+    cudaError_t e = cudaSuccess;
     for (int s0 = 0; s0 < n && e == cudaSuccess; s0 += chunk) {
         const int B = std::min(chunk, n - s0);
         e = cudaMemcpyAsync(dX, X + (size_t)s0 * din, (size_t)B * din * sizeof(float), cudaMemcpyHostToDevice, s);
+        const bf16 *x0 = nullptr;
         for (int j = 0; j < count && e == cudaSuccess; j++) {
             pt_mlp *q = members[j];
             const cudaStream_t own = q->stream;
             q->stream = s;
-            k_gather<<<B, 128, 0, s>>>(dX, nullptr, nullptr, B, din, dout, q->H[0], nullptr);
-            e = forward_infer(q, B);
-            if (e == cudaSuccess) {
-                const long long total = (long long)B * dout;
-                k_accumulate<<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, s>>>(
-                    acc, q->Z[q->L - 1], total, 1.0f / (float)count, j == 0);
-                e = cudaGetLastError();
-            }
+            e = forward_infer(q, B, dX, &x0, acc, m->ldz, 1.0f / (float)count, j == 0);
             q->stream = own;
         }
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(Y + (size_t)s0 * dout, acc, (size_t)B * dout * sizeof(float), cudaMemcpyDeviceToHost,
-                                s);
+            e = copy_out(acc, m->ldz, m->Z[m->L - 1], B, dout, Y + (size_t)s0 * dout, cudaMemcpyDeviceToHost, s);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cudaFree(dX);
-    if (acc) cudaFree(acc);
     MCK(e, "ensemble predict");
     for (int j = 0; j < count; j++) {
         const pt_status st = umma_check(members[j]);
@@ -935,23 +1337,22 @@ pt_status pt_mlp_predict_ensemble_device(pt_mlp *const *members, int count, cons
     const cudaStream_t s = m->stream;
     for (int j = 1; j < count; j++)
         if (members[j]->stream != s) MCK(cudaStreamSynchronize(members[j]->stream), "ensemble member stream");
+    MCK(ensure_zout(m), "inference output");
     for (int s0 = 0; s0 < n; s0 += chunk) {
         const int B = std::min(chunk, n - s0);
+        const bf16 *x0 = nullptr;
         for (int j = 0; j < count; j++) {
             pt_mlp *q = members[j];
             const cudaStream_t own = q->stream;
             q->stream = s;
-            k_gather<<<B, 128, 0, s>>>(X + (size_t)s0 * din, nullptr, nullptr, B, din, dout, q->H[0], nullptr);
-            cudaError_t e = forward_infer(q, B);
-            if (e == cudaSuccess) {
-                const long long total = (long long)B * dout;
-                k_accumulate<<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, s>>>(
-                    Y + (size_t)s0 * dout, q->Z[q->L - 1], total, 1.0f / (float)count, j == 0);
-                e = cudaGetLastError();
-            }
+            const cudaError_t e =
+                forward_infer(q, B, X + (size_t)s0 * din, &x0, m->zout, m->ldz, 1.0f / (float)count, j == 0);
             q->stream = own;
             MCK(e, "ensemble predict (device)");
         }
+        // the mean, from the padded accumulator into y's rows
+        MCK(copy_out(m->zout, m->ldz, nullptr, B, dout, Y + (size_t)s0 * dout, cudaMemcpyDeviceToDevice, s),
+            "ensemble mean");
     }
     return PT_OK;
 }

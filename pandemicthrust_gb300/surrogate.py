@@ -568,11 +568,12 @@ def search(surrogate, persons=50_000_000, candidates=100_000, budget_days=28, to
     judges the surrogate (peak height and attack rate errors against the replicate
     mean, over every judged scenario and strain) and makes the final choice (the
     fallback: the simulator's best, not the surrogate's, is returned).  The best
-    scenarios often stop the epidemic early, so `transfer_sample` candidates drawn at
-    random from all of them are simulated the same way and their errors reported
-    apart: the surrogate's error at this population over the whole range (pairs with
-    a simulated attack rate of at least 1%).  Returns a dict of the timings, errors and
-    choices."""
+    scenarios often stop the epidemic early, and so do most candidates of the search
+    (R 1.5 / 1.2 with 20% vaccinated), so `transfer_sample` scenarios drawn from the
+    surrogate's whole training ranges are simulated the same way at `persons` and
+    their errors reported apart: the error of the model trained at its own population
+    when carried to this one (pairs with a simulated attack rate of at least 1%).
+    Returns a dict of the timings, errors and choices."""
     rng = np.random.default_rng(seed)
     scen = search_scenarios(candidates, rng, budget_days, vaccination)
     X = features(scen)
@@ -585,19 +586,22 @@ def search(surrogate, persons=50_000_000, candidates=100_000, budget_days=28, to
     order = np.argsort(score, kind="stable")
     top = order[:max(1, int(round(candidates * top_fraction)))]
     judged = top if judge_top is None else top[:max(1, int(judge_top))]
-    sample = rng.choice(candidates, size=min(int(transfer_sample), candidates), replace=False) \
-        if transfer_sample else np.zeros(0, np.int64)
-    idx = np.concatenate([judged, sample]).astype(np.int64)
-    big = [scaled(scen[i], persons, surrogate.persons) for i in idx]
+    sample = sample_scenarios(int(transfer_sample), rng) if transfer_sample else []
+    pred_sample = transfer(decode(surrogate.raw_features(features(sample)), surrogate.persons), persons,
+                           surrogate.persons) if sample else None
+    big = [scaled(scen[i], persons, surrogate.persons) for i in judged] + \
+        [scaled(x, persons, surrogate.persons) for x in sample]
     t0 = time.time()
     sim = simulate(big, replicates, persons, seed_base=seed_base, max_persons_per_batch=max_persons_per_batch)
     t_sim = time.time() - t0
     truth = truth_summary(sim)
     nj = len(judged)
 
-    def errs(rows, min_attack):
-        sub = {k: np.asarray(v)[idx[rows]] for k, v in pred.items()}
-        t = {k: v[rows] for k, v in truth.items()}
+    def errs(p, rows_pred, rows_truth, min_attack):
+        if p is None:
+            return {"pairs": 0, "min_attack": min_attack}
+        sub = {k: np.asarray(v)[rows_pred] for k, v in p.items()}
+        t = {k: v[rows_truth] for k, v in truth.items()}
         pk, at = relative_errors(predicted_summary(sub), t, min_attack)
         if not len(pk):
             return {"pairs": 0, "min_attack": min_attack}
@@ -613,10 +617,11 @@ def search(surrogate, persons=50_000_000, candidates=100_000, budget_days=28, to
         "vaccination": vaccination,
         "top": int(len(top)), "judged": nj, "transfer_sample": int(len(sample)), "replicates": replicates,
         "surrogate_scenarios_per_s": candidates / t_score, "surrogate_seconds": t_score,
-        "abm_seconds": t_sim, "abm_runs": int(len(idx) * replicates),
+        "abm_seconds": t_sim, "abm_runs": int(len(big) * replicates),
         "abm_person_days_per_s": person_days / t_sim,
-        "error_judged": errs(np.arange(nj), 0.0),
-        "error_transfer": errs(np.arange(nj, len(idx)), 0.01),
+        "error_judged": errs(pred, judged, np.arange(nj), 0.0),
+        "error_transfer": errs(pred_sample, np.arange(len(sample)), np.arange(nj, len(big)), 0.01),
+        "transfer_scenarios": sample,
         "surrogate_choice": dict(scen[int(judged[0])], predicted_attack=[float(x) for x in pred["attack"][judged[0]]],
                                  simulated_attack=[float(x) for x in truth["attack"][0]]),
         "abm_choice": dict(scen[int(judged[best_abm])], simulated_attack=[float(x) for x in truth["attack"][best_abm]]),
@@ -659,6 +664,7 @@ def main(argv=None):
     f.add_argument("--rows", type=int, default=262144)
     f.add_argument("--repeats", type=int, default=3)
     f.add_argument("--mma-sync", action="store_true", help="the mma.sync kernel instead of tcgen05")
+    f.add_argument("--chunk", type=int, default=262144, help="rows per inference launch")
     q = sub.add_parser("search")
     q.add_argument("--model", default=SHIPPED_MODEL)
     q.add_argument("--persons", type=int, default=50_000_000)
@@ -687,7 +693,7 @@ def main(argv=None):
         s.close()
         print(json.dumps(info))
     elif a.cmd == "infer":
-        s = Surrogate.load(a.model, max_batch=65536)
+        s = Surrogate.load(a.model, max_batch=a.chunk)
         for net in s.nets:
             net.set_tcgen05(not a.mma_sync)
         X = features(sample_scenarios(a.rows, np.random.default_rng(5)))
@@ -696,9 +702,28 @@ def main(argv=None):
             t0 = time.time()
             s.raw_features(X)
             times.append(time.time() - t0)
+        # device time with inputs and outputs resident (CUDA events on the networks'
+        # stream, the legacy default stream)
+        device = []
+        try:
+            import torch
+            xd = torch.from_numpy(X).cuda()
+            yd = torch.empty((len(X), OUTPUTS), dtype=torch.float32, device="cuda")
+            s.raw_device(xd.data_ptr(), len(X), yd.data_ptr())
+            for _ in range(a.repeats):
+                ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                ev0.record(torch.cuda.default_stream())
+                s.raw_device(xd.data_ptr(), len(X), yd.data_ptr())
+                ev1.record(torch.cuda.default_stream())
+                torch.cuda.synchronize()
+                device.append(ev0.elapsed_time(ev1) / 1000.0)
+        except ImportError:
+            pass
         s.close()
         print(json.dumps({"rows": a.rows, "members": len(s.nets), "kernel": "mma.sync" if a.mma_sync else "tcgen05",
-                          "seconds": times, "scenarios_per_s": a.rows / min(times)}))
+                          "chunk": a.chunk,
+                          "seconds": times, "scenarios_per_s": a.rows / min(times), "device_seconds": device,
+                          "device_scenarios_per_s": a.rows / min(device) if device else None}))
     elif a.cmd == "search":
         s = Surrogate.load(a.model, max_batch=65536)
         r = search(s, a.persons, a.candidates, a.budget_days, a.top_fraction, a.judge_top, a.replicates, a.seed)

@@ -177,6 +177,7 @@ def test_intervention_search_screens_then_judges_with_the_simulator(native_lib):
                   replicates=3, transfer_sample=2, seed_base=400_000_000)
     s.close()
     assert r["candidates"] == 3000 and r["top"] == 30 and r["judged"] == 2 and r["transfer_sample"] == 2
+    assert len(r["transfer_scenarios"]) == 2 and all(sg.in_range(r["transfer_scenarios"]))
     assert r["abm_runs"] == 12 and r["abm_person_days_per_s"] > 0 and r["surrogate_scenarios_per_s"] > 0
     assert r["abm_choice"]["closure_days"] <= 14 and r["abm_choice"]["vaccination"] == 0.2
     assert r["seeds_at_persons"] == 6   # 20 per million, scaled to 300,000 persons

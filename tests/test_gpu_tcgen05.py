@@ -36,10 +36,11 @@ def reference_forward(params, widths, X):
     return H
 
 
-@pytest.mark.parametrize("widths,rows", [([11, 256, 256, 256, 256, 222], 1000),     # the surrogate's shape
+@pytest.mark.parametrize("widths,rows", [([11, 256, 256, 256, 256, 222], 1000),   # the surrogate's shape
                                           ([11, 256, 256, 256, 256, 222], 128),
                                           ([16, 64, 32], 300),
-                                          ([40, 128, 256, 96], 4100)])
+                                          ([40, 128, 256, 96], 4100),
+                                          ([160, 192, 48], 777)])   # K stages of 80 + 80 and 128 + 64
 def test_tcgen05_forward_matches_reference_and_mma_sync(native_lib, widths, rows):
     rng = np.random.default_rng(11)
     net = sg.MLP(widths, max_batch=4096, seed=5)
