@@ -226,6 +226,18 @@ pt_status pt_autotune(pt_sim *sim, int days, pt_tuning *chosen);
  * PT_ERR_ARG.  Allocates and frees 64 bytes of device memory; synchronises the device. */
 pt_status pt_selftest_bounded_wait(int publish_predecessor, int64_t spin_limit, uint32_t *prefix);
 
+/* Checks the schedule kernels' errand lookup against the reference's form of it
+ * (device_fishAfterschoolOrErrandDestination_weekday, PandemicSim.cu:2909-2947, and
+ * device_fishWeekendErrandDestination, :1017-1044: a loop over the errand types and
+ * an IEEE division).  The kernels search without branches and divide by multiplying
+ * with the reciprocal and one correction step.  counts receives: [0] weekday and [1]
+ * weekend random words (all 2^32) whose errand type or quotient differs; [2] pairs
+ * (x, probability) with x = 0 or any float in [2^-32, 1] (the values the search
+ * divides) whose quotient differs from the IEEE division; [3] reciprocal table
+ * entries that are not the rounded reciprocal.  All
+ * zero is a pass.  Runs one kernel of about 2^32 iterations; synchronises the device. */
+pt_status pt_selftest_errand_lookup(uint64_t counts[4]);
+
 /* Kernel launches issued by this library in the calling process so far. */
 uint64_t pt_launch_count(void);
 

@@ -22,6 +22,15 @@ static __constant__ float c_weekday_errand_pdf[kTypes] = {0, 0, 0, 0, 0, 0, 0, 0
                                                    0.61919f, 0, 0.27812f, 0.06601f, 0.03668f};
 static __constant__ float c_weekend_errand_pdf[kTypes] = {0, 0, 0, 0, 0, 0, 0, 0, 0,
                                                    0.51493f, 0, 0.25586f, 0.1162f, 0.113f};
+// The reciprocals of the errand probabilities, rounded to nearest (each quotient
+// folded by the compiler in IEEE single precision; 0 where the probability is 0,
+// a row the search below never ends on).
+static __constant__ float c_weekday_errand_rcp[kTypes] = {0, 0, 0, 0, 0, 0, 0, 0, 0,
+                                                   1.0f / 0.61919f, 0, 1.0f / 0.27812f, 1.0f / 0.06601f,
+                                                   1.0f / 0.03668f};
+static __constant__ float c_weekend_errand_rcp[kTypes] = {0, 0, 0, 0, 0, 0, 0, 0, 0,
+                                                   1.0f / 0.51493f, 0, 1.0f / 0.25586f, 1.0f / 0.1162f,
+                                                   1.0f / 0.113f};
 static __constant__ int c_hh_adults[9] = {1, 1, 2, 1, 2, 1, 2, 1, 2};
 static __constant__ int c_hh_children[9] = {0, 1, 0, 2, 1, 3, 2, 4, 3};
 static __constant__ float c_hh_cdf[9] = {0.279f, 0.319f, 0.628f, 0.671f, 0.8f, 0.812f, 0.939f, 0.944f, 1.0f};
@@ -254,22 +263,74 @@ __device__ __forceinline__ int fish_school_and_age(const SimConst &c, uint32_t r
     return business_in_type(c, frac, row + 3);
 }
 
+// x / d rounded to nearest, for the errand probabilities d with r = RN(1/d): one
+// multiply and Markstein's correction (P. Markstein, IBM J. Res. Dev. 34(1), 1990):
+// q = RN(x r), e = x - q d exactly (a fused multiply-add), RN(q + e r).  It equals
+// __fdiv_rn(x, d) for x = 0 and every float x in [2^-32, 1] (the values the errand
+// search divides) and every row the search can end on; pt_selftest_errand_lookup
+// checks all of them, and the whole search on every 32-bit draw.
+__device__ __forceinline__ float div_rn_recip(float x, float d, float r)
+{
+    const float q = __fmul_rn(x, r);
+    const float e = __fmaf_rn(-q, d, x);
+    return __fmaf_rn(e, r, q);
+}
+
+// The errand-type search of device_fishAfterschoolOrErrandDestination_weekday (its
+// adult branch, PandemicSim.cu:2909-2947) and device_fishWeekendErrandDestination
+// (PandemicSim.cu:1017-1044):
+//     row = 9; while (y > pdf[row] && row < 13) { y = y - pdf[row]; row++; }
+//     frac = y / pdf[row];
+// without branches.  The chain of subtractions runs to the end and the stop is
+// selected: once y <= pdf[t], every later remainder is <= 0 (the probabilities are
+// >= 0), so every later test fails too, as the loop would have stopped.  Returns the
+// row; frac receives the quotient.
+template <bool WEEKEND>
+__device__ __forceinline__ int errand_row(float y, float &frac)
+{
+    const float *pdf = WEEKEND ? c_weekend_errand_pdf : c_weekday_errand_pdf;
+    const float *rcp = WEEKEND ? c_weekend_errand_rcp : c_weekday_errand_rcp;
+    float x = y, d = pdf[9], rd = rcp[9], f = y;
+    int row = 9;
+#pragma unroll
+    for (int t = 9; t < kTypes - 1; t++) {
+        const bool go = f > pdf[t];
+        f = __fsub_rn(f, pdf[t]);
+        row = go ? t + 1 : row;
+        x = go ? f : x;
+        d = go ? pdf[t + 1] : d;
+        rd = go ? rcp[t + 1] : rd;
+    }
+    frac = div_rn_recip(x, d, rd);
+    return row;
+}
+
+// The same search as the reference writes it: the loop and the IEEE division.  Kept
+// as the self-test's reference for errand_row.
+template <bool WEEKEND>
+__device__ __forceinline__ int errand_row_loop(float y, float &frac)
+{
+    const float *pdf = WEEKEND ? c_weekend_errand_pdf : c_weekday_errand_pdf;
+    int row = 9;
+    while (y > pdf[row] && row < kTypes - 1) {
+        y = __fsub_rn(y, pdf[row]);
+        row++;
+    }
+    frac = __fdiv_rn(y, pdf[row]);
+    return row;
+}
+
 // device_fishAfterschoolOrErrandDestination_weekday, PandemicSim.cu:2909-2947
-// (unsigned business number, as the reference).
+// (unsigned business number, as the reference).  Children go to an afterschool
+// location (type 8); adults to an errand type drawn by errand_row.  Both are computed
+// and one is selected, so a warp of adults and children does not diverge.
 __device__ __forceinline__ int fish_weekday_dest(const SimConst &c, uint32_t r, bool adult)
 {
-    int type = 8;  // BUSINESS_TYPE_AFTERSCHOOL
-    float frac = to_unit(r);
-    if (adult) {
-        type = 9;
-        float row_pdf = c_weekday_errand_pdf[type];
-        while (frac > row_pdf && type < kTypes - 1) {
-            frac = __fsub_rn(frac, row_pdf);
-            type++;
-            row_pdf = c_weekday_errand_pdf[type];
-        }
-        frac = __fdiv_rn(frac, row_pdf);
-    }
+    const float y = to_unit(r);
+    float fa;
+    const int ta = errand_row<false>(y, fa);
+    const int type = adult ? ta : 8;   // 8: BUSINESS_TYPE_AFTERSCHOOL
+    const float frac = adult ? fa : y;
     int count = c.type_count[type];
     unsigned int b = __float2uint_rz(__fmul_rn(frac, __int2float_rn(count)));
     if (b >= (unsigned int)count) b = (unsigned int)(count - 1);
@@ -280,13 +341,9 @@ __device__ __forceinline__ int fish_weekday_dest(const SimConst &c, uint32_t r, 
 // device_fishWeekendErrandDestination, PandemicSim.cu:1017-1044
 __device__ __forceinline__ int fish_weekend_dest(const SimConst &c, uint32_t r)
 {
-    float y = to_unit(r);
-    int row = 9;
-    while (y > c_weekend_errand_pdf[row] && row < kTypes - 1) {
-        y = __fsub_rn(y, c_weekend_errand_pdf[row]);
-        row++;
-    }
-    return business_in_type(c, __fdiv_rn(y, c_weekend_errand_pdf[row]), row);
+    float frac;
+    const int row = errand_row<true>(to_unit(r), frac);
+    return business_in_type(c, frac, row);
 }
 
 // device_generateWeekendErrands, PandemicSim.cu:980-1014: three distinct hours of

@@ -1095,8 +1095,10 @@ cudaError_t launch_infected_list(const DevArrays &d, cudaStream_t s)
 __device__ __forceinline__ void weekday_pair_keys(const SimConst &c, const uint32_t w[4], int k, bool adult, int lo,
                                                   int R, int &k1, int &k2)
 {
-    int d1 = fish_weekday_dest(c, w[2 * k], adult);
-    int d2 = adult ? fish_weekday_dest(c, w[2 * k + 1], true) : d1;
+    // the second errand is drawn for every lane and kept for adults (no divergence)
+    const int d1 = fish_weekday_dest(c, w[2 * k], adult);
+    const int e2 = fish_weekday_dest(c, w[2 * k + 1], true);
+    const int d2 = adult ? e2 : d1;
     k1 = d1 - lo;
     k2 = R + d2 - lo;
 }
@@ -2083,6 +2085,65 @@ cudaError_t launch_wait_probe(unsigned long long *tiles, int *error, int publish
 }
 
 long long max_spin_limit() { return kSpinLimit; }
+
+// ================================================================== errand-lookup self-test
+// The schedule kernels' branch-free errand search (errand_row) against the reference's
+// loop and IEEE division (errand_row_loop), on every 32-bit random word the schedule
+// can draw: counts[0] weekday and counts[1] weekend words whose row or quotient bits
+// differ.  counts[2]: floats x in the domain the search divides, 0 and [2^-32, 1]
+// (a draw is 0 or at least 2^-32, a remainder after a subtraction at least 2^-28), and
+// errand rows r in {9, 11, 12, 13} of both tables where div_rn_recip(x, pdf[r], rcp[r])
+// differs from __fdiv_rn(x, pdf[r]).  (Below about 2^-100 the correction step's
+// remainder underflows and the two can differ; no draw gets there.)  counts[3]:
+// reciprocal table entries that differ from __frcp_rn of their probability.
+__global__ void k_errand_selftest(unsigned long long *counts)
+{
+    unsigned long long bad_wd = 0, bad_we = 0, bad_div = 0;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < (1ull << 32);
+         i += stride) {
+        const float y = to_unit((uint32_t)i);
+        float a, b;
+        int ra = errand_row<false>(y, a), rb = errand_row_loop<false>(y, b);
+        bad_wd += (ra != rb || __float_as_uint(a) != __float_as_uint(b)) ? 1 : 0;
+        ra = errand_row<true>(y, a);
+        rb = errand_row_loop<true>(y, b);
+        bad_we += (ra != rb || __float_as_uint(a) != __float_as_uint(b)) ? 1 : 0;
+        if (i == 0 || (i >= 0x2F800000ull && i <= 0x3F800000ull)) {   // 0 and [2^-32, 1]
+            const float x = __uint_as_float((uint32_t)i);
+            const int rows[4] = {9, 11, 12, 13};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int r = rows[k];
+                bad_div += __float_as_uint(div_rn_recip(x, c_weekday_errand_pdf[r], c_weekday_errand_rcp[r])) !=
+                                   __float_as_uint(__fdiv_rn(x, c_weekday_errand_pdf[r]))
+                               ? 1
+                               : 0;
+                bad_div += __float_as_uint(div_rn_recip(x, c_weekend_errand_pdf[r], c_weekend_errand_rcp[r])) !=
+                                   __float_as_uint(__fdiv_rn(x, c_weekend_errand_pdf[r]))
+                               ? 1
+                               : 0;
+            }
+        }
+    }
+    if (bad_wd) atomicAdd(&counts[0], bad_wd);
+    if (bad_we) atomicAdd(&counts[1], bad_we);
+    if (bad_div) atomicAdd(&counts[2], bad_div);
+    if (blockIdx.x == 0 && threadIdx.x < kTypes) {
+        const int t = threadIdx.x;
+        unsigned long long bad = 0;
+        if (c_weekday_errand_pdf[t] > 0.f && c_weekday_errand_rcp[t] != __frcp_rn(c_weekday_errand_pdf[t])) bad++;
+        if (c_weekend_errand_pdf[t] > 0.f && c_weekend_errand_rcp[t] != __frcp_rn(c_weekend_errand_pdf[t])) bad++;
+        if (bad) atomicAdd(&counts[3], bad);
+    }
+}
+
+cudaError_t launch_errand_selftest(unsigned long long *counts, cudaStream_t s)
+{
+    k_errand_selftest<<<sm_count() * 8, 256, 0, s>>>(counts);
+    count_launch();
+    return cudaGetLastError();
+}
 
 // ================================================================== final
 // final_countReproduction's generation counts (PandemicSim.cu:2227-2304) for every

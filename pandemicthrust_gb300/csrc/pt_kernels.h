@@ -252,6 +252,8 @@ cudaError_t launch_gen_hist(const DevArrays &d, int *hist, cudaStream_t s);
 // ---- the bounded look-back wait in isolation (tiles: 2 zeroed words; error: zeroed)
 cudaError_t launch_wait_probe(unsigned long long *tiles, int *error, int publish_first, long long spin_limit,
                               unsigned *prefix_out, cudaStream_t s);
+// The errand-lookup self-test: counts[4] (zeroed by the caller) receive mismatch counts.
+cudaError_t launch_errand_selftest(unsigned long long *counts, cudaStream_t s);
 long long max_spin_limit();   // the polls every wait of the simulation allows
 
 uint64_t launches();

@@ -1213,6 +1213,22 @@ pt_status pt_selftest_bounded_wait(int publish_predecessor, int64_t spin_limit, 
     return PT_OK;
 }
 
+pt_status pt_selftest_errand_lookup(uint64_t counts[4])
+{
+    if (!counts) return PT_ERR_ARG;
+    unsigned long long *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, 4 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc(errand self-test)");
+    unsigned long long h[4] = {0, 0, 0, 0};
+    e = cudaMemset(d, 0, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = ptk::launch_errand_selftest(d, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "errand self-test");
+    for (int i = 0; i < 4; i++) counts[i] = h[i];
+    return PT_OK;
+}
+
 void pt_destroy(pt_sim *s) { delete s; }
 
 const char *pt_last_error(const pt_sim *s)
