@@ -277,8 +277,9 @@ pt_status pt_bucket_table_static(const int32_t *keys, int n, int buckets, int32_
  * The multilayer perceptron behind the learned surrogate (no counterpart in the
  * reference): BF16 weights and activations, FP32 accumulation, FP32 master weights
  * and Adam, trained and evaluated by this library's own kernels.  layers linear
- * maps widths[0] -> widths[1] -> ... -> widths[layers]; GELU after every hidden layer,
- * none after the last.  Parameters are one float array, layer by layer: W (out x in,
+ * maps widths[0] -> widths[1] -> ... -> widths[layers]; GELU after every hidden layer
+ * (its tanh form, 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))), with the hardware
+ * tanh), none after the last.  Parameters are one float array, layer by layer: W (out x in,
  * row-major) then b (out).  The loss is the mean squared error over a batch. */
 typedef struct pt_mlp pt_mlp;
 
@@ -305,9 +306,8 @@ pt_status pt_mlp_predict_ensemble_device(pt_mlp *const *members, int count, cons
  * operand loads into shared memory, FP32 accumulators in tensor memory) when every
  * layer is at most 256 wide and hidden widths are multiples of 32; enabled = 0
  * selects the warp-level mma.sync kernel that training uses.  Both accumulate in FP32
- * and round activations to BF16.  The tcgen05 epilogue evaluates GELU in a
- * polynomial-exponential form within 1.5e-7 of the erf form the mma.sync kernel uses,
- * so the paths agree to FP32 summation order and that difference. */
+ * and round activations to BF16, and both evaluate the same activation step by step,
+ * so they agree to FP32 summation order. */
 pt_status pt_mlp_set_tcgen05(pt_mlp *mlp, int enabled);
 void pt_mlp_destroy(pt_mlp *mlp);
 const char *pt_mlp_last_error(const pt_mlp *mlp);

@@ -58,12 +58,35 @@ struct GemmArgs {
     bf16 *dZb;
 };
 
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+// The activation: GELU in its tanh form (Hendrycks and Gimpel, arXiv:1606.08415),
+// 0.5 z (1 + tanh(u)), u = sqrt(2/pi) (z + 0.044715 z^3), with the hardware tanh
+// (tanh.approx.f32).  Training and inference evaluate the same expression.
+constexpr float kGeluC0 = 0.7978845608028654f;               // sqrt(2 / pi)
+constexpr float kGeluC1 = 0.7978845608028654f * 0.044715f;   // sqrt(2 / pi) * 0.044715
+
+__device__ __forceinline__ float tanh_approx(float x)
+{
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// rounded step by step as the tcgen05 epilogue's paired form (gelu_bf16x2):
+// w = c0 + c1 z^2, t = tanh(w z), h = z / 2, h + h t
+__device__ __forceinline__ float gelu(float z)
+{
+    const float w = __fmaf_rn(__fmul_rn(z, z), kGeluC1, kGeluC0);
+    const float t = tanh_approx(__fmul_rn(w, z));
+    const float h = __fmul_rn(0.5f, z);
+    return __fmaf_rn(h, t, h);
+}
 
 __device__ __forceinline__ float gelu_grad(float z)
 {
-    // d/dz [z Phi(z)] = Phi(z) + z phi(z)
-    return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+    // d/dz [0.5 z (1 + t)] = 0.5 (1 + t) + 0.5 z (1 - t^2) du/dz, du/dz = c0 + 3 c1 z^2
+    const float z2 = z * z;
+    const float t = tanh_approx(z * (kGeluC0 + kGeluC1 * z2));
+    return 0.5f * (1.f + t) + 0.5f * z * (1.f - t * t) * (kGeluC0 + 3.f * kGeluC1 * z2);
 }
 
 __device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi)
@@ -201,14 +224,6 @@ constexpr int kUmmaEpiWarps = 8;               // epilogue warps: two per lane q
 constexpr long long kUmmaSpin = 1ll << 22;     // polls of an mbarrier before a wait gives up
 static_assert(kUmmaSmem <= 227 * 1024, "the tcgen05 layer needs more shared memory than a CTA has");
 
-// The epilogue's GELU: max(z, 0) - a 2^p(-a), a = min(|z|, kGeluClamp), p a degree-7
-// polynomial for log2(Phi(-a)) (coefficients of (-a)^k, from fit_gelu.py beside this
-// file).  Equal to z Phi(z) within 1.5e-7 absolute on every z; the exp2 is ex2.approx.
-constexpr float kGelu0 = -9.999998808e-01f, kGelu1 = 1.151111007e+00f, kGelu2 = -4.591529965e-01f,
-                kGelu3 = 5.269147828e-02f, kGelu4 = 7.389675826e-03f, kGelu5 = 4.214611836e-04f,
-                kGelu6 = -5.384269025e-05f, kGelu7 = -8.463827726e-06f;
-constexpr float kGeluClamp = 5.656854153e+00f;
-
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // two FP32 lanes in one 64-bit register, for the paired FP32 instructions (f32x2)
@@ -238,11 +253,11 @@ __device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b)
     return d;
 }
 
-__device__ __forceinline__ float ex2_approx(float x)
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b)
 {
-    float y;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
 }
 
 // BF16 pair, lo in the low half (round to nearest even)
@@ -253,24 +268,16 @@ __device__ __forceinline__ uint32_t bf16x2(float lo, float hi)
     return d;
 }
 
-// GELU of a pair of pre-activations, packed to BF16
+// GELU (the tanh form above) of a pair of pre-activations, packed to BF16: four
+// paired FP32 instructions and two tanh per pair
 __device__ __forceinline__ uint32_t gelu_bf16x2(uint64_t z)
 {
-    float z0, z1;
-    f2_split(z, z0, z1);
-    const float n0 = fmaxf(-fabsf(z0), -kGeluClamp), n1 = fmaxf(-fabsf(z1), -kGeluClamp);   // -a
-    const uint64_t n = f2(n0, n1);
-    uint64_t p = f2_fma(f2(kGelu7, kGelu7), n, f2(kGelu6, kGelu6));
-    p = f2_fma(p, n, f2(kGelu5, kGelu5));
-    p = f2_fma(p, n, f2(kGelu4, kGelu4));
-    p = f2_fma(p, n, f2(kGelu3, kGelu3));
-    p = f2_fma(p, n, f2(kGelu2, kGelu2));
-    p = f2_fma(p, n, f2(kGelu1, kGelu1));
-    p = f2_fma(p, n, f2(kGelu0, kGelu0));
-    float p0, p1;
-    f2_split(p, p0, p1);
+    const uint64_t w = f2_fma(f2_mul(z, z), f2(kGeluC1, kGeluC1), f2(kGeluC0, kGeluC0));   // c0 + c1 z^2
+    float u0, u1;
+    f2_split(f2_mul(w, z), u0, u1);
+    const uint64_t h = f2_mul(z, f2(0.5f, 0.5f));
     float r0, r1;
-    f2_split(f2_fma(n, f2(ex2_approx(p0), ex2_approx(p1)), f2(fmaxf(z0, 0.f), fmaxf(z1, 0.f))), r0, r1);
+    f2_split(f2_fma(h, f2(tanh_approx(u0), tanh_approx(u1)), h), r0, r1);   // h (1 + t)
     return bf16x2(r0, r1);
 }
 

@@ -32,6 +32,9 @@ OUTPUTS = 2 * DAYS + 6 + 2 * GENERATIONS
 # up so the squared error weighs them as much as the 200 daily values together
 SUMMARY_WEIGHT = 5.0
 EXPECTED_HOUSEHOLD_SIZE = 2.354
+# the hidden layers' activation, as the kernels evaluate it (pt_mlp.cu): a saved
+# network trained with another one is refused
+ACTIVATION = "gelu_tanh"
 
 # scenario ranges (inclusive); seeds are sampled and encoded on a log scale
 RANGES = {
@@ -456,7 +459,7 @@ def _encoding():
     """What a saved surrogate must share with this module: its inputs and targets."""
     return dict(features=list(FEATURES), ranges={k: list(v) for k, v in RANGES.items()}, days=DAYS,
                 generations=GENERATIONS, rn_scale=RN_SCALE, summary_weight=SUMMARY_WEIGHT, n_derived=N_DERIVED,
-                outputs=OUTPUTS)
+                outputs=OUTPUTS, activation=ACTIVATION)
 
 
 def _bias_mask(widths):

@@ -4,7 +4,6 @@ method without it (nearest neighbour in the training set), judged by the mean of
 simulator replicates."""
 import numpy as np
 import pytest
-from scipy.special import erf
 
 from pandemicthrust_gb300 import surrogate as sg
 
@@ -18,12 +17,17 @@ def bf16(x):
     return u.view(np.float32).astype(np.float64)
 
 
+C0, C1 = np.sqrt(2 / np.pi), np.sqrt(2 / np.pi) * 0.044715
+
+
 def gelu(z):
-    return 0.5 * z * (1 + erf(z / np.sqrt(2)))
+    """GELU in its tanh form, as the kernels (which use the hardware tanh)."""
+    return 0.5 * z * (1 + np.tanh(z * (C0 + C1 * z * z)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1 + erf(z / np.sqrt(2))) + z * np.exp(-0.5 * z * z) / np.sqrt(2 * np.pi)
+    t = np.tanh(z * (C0 + C1 * z * z))
+    return 0.5 * (1 + t) + 0.5 * z * (1 - t * t) * (C0 + 3 * C1 * z * z)
 
 
 def reference_gradients(params, widths, X, Y):
