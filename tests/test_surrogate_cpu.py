@@ -45,6 +45,7 @@ def test_shipped_model_matches_this_module():
     assert meta["features"] == list(sg.FEATURES)
     assert meta["ranges"] == {k: list(v) for k, v in sg.RANGES.items()}
     assert meta["outputs"] == sg.OUTPUTS and meta["summary_weight"] == sg.SUMMARY_WEIGHT
+    assert meta["activation"] == sg.ACTIVATION
     w = meta["widths"]
     n = sum(w[i] * w[i + 1] + w[i + 1] for i in range(len(w) - 1))
     assert z["params"].shape == (meta["members"], n) and z["params"].dtype == np.uint16
@@ -100,9 +101,10 @@ def test_load_refuses_a_model_for_other_targets(tmp_path):
     meta = dict(sg._encoding(), persons=1000, widths=[len(sg.FEATURES) + sg.N_DERIVED, 8, sg.OUTPUTS], members=1,
                 info={})
     for key, value in (("summary_weight", sg.SUMMARY_WEIGHT + 1.0), ("days", sg.DAYS + 1),
-                       ("ranges", dict(meta["ranges"], vaccination=[0.0, 0.9]))):
+                       ("ranges", dict(meta["ranges"], vaccination=[0.0, 0.9])),
+                       ("activation", "gelu_erf"), ("activation", None)):   # None: a file from before the key
         bad = dict(meta, **{key: value})
-        path = tmp_path / ("bad_%s.npz" % key)
+        path = tmp_path / ("bad_%s_%s.npz" % (key, value is None))
         np.savez(path, params=np.zeros((1, 10), np.uint16), biases=np.zeros((1, 10), np.float32),
                  meta=np.array(json.dumps(bad)))
         with pytest.raises(ValueError, match=key):
