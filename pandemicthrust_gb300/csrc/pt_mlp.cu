@@ -626,6 +626,179 @@ __global__ void __launch_bounds__(32 * (2 + EPI), 1)
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
 }
 
+// ---------------------------------------------------------------- ensemble mean layer
+// The members' last layers in one GEMM: y = inv * (sum_m W_m h_m + sum_m b_m), the
+// mean of the members' outputs.  The members' last hidden activations h_m (M x Kh BF16
+// each) are one operand concatenated along K, their weights W_m (Np x Kh) side by
+// side in Wc (Np x members * Kh), so the tensor cores sum over members in the
+// accumulator and the outputs are written once (instead of a read-modify-write of an
+// FP32 accumulator per member).  Wc is too large for shared memory, so every stage of
+// the ring carries a 64-column slice of both operands (128-byte swizzled boxes); the
+// roles, accumulators, waits and epilogue are those of k_umma_layer.
+constexpr int kMeanMaxMembers = 8;
+constexpr int kMeanStages = 4;
+constexpr int kMeanAStage = kUmmaM * 64 * 2;        // 16 KB
+constexpr int kMeanWStage = kUmmaMaxN * 64 * 2;     // 32 KB
+constexpr int kMeanSmem = kUmmaBarBytes + kUmmaBiasBytes + kMeanStages * (kMeanAStage + kMeanWStage);
+static_assert(kMeanSmem <= 227 * 1024, "the ensemble layer needs more shared memory than a CTA has");
+
+struct MeanMaps {
+    CUtensorMap a[kMeanMaxMembers];   // member m's hidden activations, box 64 x kUmmaM, 128-byte swizzle
+};
+
+template <int EPI>
+__global__ void __launch_bounds__(32 * (2 + EPI), 1)
+    k_umma_mean_layer(const __grid_constant__ MeanMaps maps, const __grid_constant__ CUtensorMap tmW, int M, int Kh,
+                      int members, int Np, int N, const float *bias_sum, float inv, float *Y, long long ldy, int vec,
+                      int *error)
+{
+    static_assert(EPI % 4 == 0, "each of the four lane quarters needs the same number of epilogue warps");
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const uint32_t b_full = smem_u32(smem), b_empty = b_full + 8 * kMeanStages, b_accf = b_empty + 8 * kMeanStages,
+                   b_acce = b_accf + 16, b_drain = b_acce + 16;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + 256);
+    volatile int *fail = reinterpret_cast<volatile int *>(smem + 320);
+    float *s_bias = reinterpret_cast<float *>(smem + kUmmaBarBytes);
+    const uint32_t sA_u = smem_u32(smem + kUmmaBarBytes + kUmmaBiasBytes);   // stage s: A at +s*(A+W), W after it
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (threadIdx.x == 32) {
+        for (int i = 0; i < kMeanStages; i++) {
+            mbar_init(b_full + 8 * i, 1);
+            mbar_init(b_empty + 8 * i, 1);
+        }
+        for (int i = 0; i < 2; i++) {
+            mbar_init(b_accf + 8 * i, 1);
+            mbar_init(b_acce + 8 * i, EPI);
+        }
+        mbar_init(b_drain, 1);
+        *fail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    for (int c = threadIdx.x; c < kUmmaMaxN; c += blockDim.x) s_bias[c] = c < N ? bias_sum[c] : 0.f;
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = *tmem_slot;
+    const int tiles = (M + kUmmaM - 1) / kUmmaM;
+    const int per = Kh / 64, nks = per * members;   // 64-column slices per member, per tile
+    const uint32_t stage_bytes = kMeanAStage + kMeanWStage;
+    if (warp == 0) {
+        if (lane == 0) {
+            // producer: per stage, the slice of one member's activations and of the weights
+            bool ok = true;
+            int it = 0;
+            for (int t = blockIdx.x; ok && t < tiles; t += gridDim.x)
+                for (int j = 0; j < nks; j++) {
+                    const int s = it % kMeanStages, use = it / kMeanStages;
+                    if (use > 0 && !mbar_wait(b_empty + 8 * s, (use - 1) & 1, fail)) {
+                        ok = false;
+                        break;
+                    }
+                    const uint32_t a = sA_u + s * stage_bytes;
+                    mbar_expect_tx(b_full + 8 * s, (uint32_t)(kUmmaM * 128 + Np * 128));
+                    tma_load_2d(a, &maps.a[j / per], 64 * (j % per), t * kUmmaM, b_full + 8 * s);
+                    tma_load_2d(a + kMeanAStage, &tmW, 64 * j, 0, b_full + 8 * s);
+                    it++;
+                }
+            if (!ok) umma_fail(fail, error);
+            for (int s = 0; s < kMeanStages; s++) {
+                const int uses = it / kMeanStages + (s < it % kMeanStages ? 1 : 0);
+                if (uses > 0) mbar_wait(b_full + 8 * s, (uses - 1) & 1, nullptr);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // MMA issuer: 4 MMAs (K = 16) per 64-column slice
+            bool ok = true;
+            const uint32_t idesc = umma_idesc(kUmmaM, Np);
+            int it = 0, tc = 0;
+            for (int t = blockIdx.x; ok && t < tiles; t += gridDim.x, tc++) {
+                const int b = tc & 1, use = tc >> 1;
+                if (use > 0 && !mbar_wait(b_acce + 8 * b, (use - 1) & 1, fail)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t d = tmem + 256u * b;
+                for (int j = 0; j < nks; j++, it++) {
+                    const int s = it % kMeanStages, u = it / kMeanStages;
+                    if (!mbar_wait(b_full + 8 * s, u & 1, fail)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t a = sA_u + s * stage_bytes, w = a + kMeanAStage;
+                    for (int q = 0; q < 4; q++)
+                        umma_bf16(d, umma_desc(a + 32 * q, 16, 1024, kSwizzle128B),
+                                  umma_desc(w + 32 * q, 16, 1024, kSwizzle128B), idesc, (j | q) != 0);
+                    umma_commit(b_empty + 8 * s);
+                }
+                if (!ok) break;
+                umma_commit(b_accf + 8 * b);
+            }
+            if (!ok) umma_fail(fail, error);
+            umma_commit(b_drain);
+            mbar_wait(b_drain, 0, nullptr);
+        }
+        __syncwarp();
+    } else {
+        // epilogue: y = inv * (acc + sum of the biases), written once
+        const int q = warp & 3, part = (warp - 2) >> 2;
+        constexpr int parts = EPI / 4;
+        int tc = 0;
+        for (int t = blockIdx.x; t < tiles; t += gridDim.x, tc++) {
+            const int b = tc & 1, use = tc >> 1;
+            if (!__all_sync(0xffffffffu, mbar_wait(b_accf + 8 * b, use & 1, fail))) {
+                if (lane == 0) umma_fail(fail, error);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const int row = t * kUmmaM + 32 * q + lane;
+            const uint32_t tb = tmem + ((uint32_t)(32 * q) << 16) + 256u * b;
+            for (int c0 = 32 * part; c0 < Np; c0 += 32 * parts) {
+                uint32_t v[32];
+                __syncwarp();
+                tmem_ld32_issue(tb + c0, v);
+                tmem_ld_wait(v);
+                if (row < M) epilogue_chunk(v, c0, row, s_bias, N, 0, nullptr, 0, Y, ldy, inv, 1, vec);
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(b_acce + 8 * b);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+}
+
+// Wc (np x members * kh): member m's padded last-layer weights in columns [m kh, (m+1) kh)
+__global__ void k_concat_weights(const bf16 *const *w, int members, int np, int kh, bf16 *wc)
+{
+    const long long n = (long long)np * kh * members;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long r = i / ((long long)kh * members);
+        const int c = (int)(i % ((long long)kh * members));
+        wc[i] = w[c / kh][r * kh + c % kh];
+    }
+}
+
+// sum over members of the last layer's biases (n outputs)
+__global__ void k_bias_sum(const float *const *b, int members, int n, float *out)
+{
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int m = 0; m < members; m++) s += b[m][c];
+        out[c] = s;
+    }
+}
+
 // Zero-padded BF16 copies for the tcgen05 path: src rows x cols (row stride cols) ->
 // dst prow x pcol.
 __global__ void k_pad_bf16(const bf16 *src, int rows, int cols, bf16 *dst, int prow, int pcol)
@@ -778,6 +951,12 @@ struct pt_mlp {
     // inference output: the last layer's outputs, rows padded to a multiple of 32
     float *zout = nullptr;
     int ldz = 0;
+    // the ensemble mean layer (held by an ensemble's first network): the members' last
+    // weights side by side, their summed biases, and device copies of the pointers
+    bf16 *wcat = nullptr;
+    float *bsum = nullptr;
+    void **mean_ptrs = nullptr;   // kMeanMaxMembers weight pointers, then as many bias pointers
+    size_t wcat_elems = 0;
 };
 
 static pt_status mfail(pt_mlp *m, pt_status st, const std::string &msg)
@@ -982,22 +1161,20 @@ static cudaError_t ensure_zout(pt_mlp *m)
 // layer accumulates in its epilogue), else forward() and k_accumulate.  *x0 caches the
 // zero-padded BF16 copy of x that the tcgen05 layers read: the first network of an
 // ensemble makes it (into its h0p), the others reuse it.
-static cudaError_t forward_infer(pt_mlp *m, int B, const float *x, const bf16 **x0, float *y, long long ldy,
-                                 float scale, bool first)
+// The tcgen05 path's per-network state: padded BF16 weights (re-padded after a
+// parameter change), the padded input buffer and the wait error word.
+static cudaError_t umma_prepare(pt_mlp *m)
 {
-    if (!m->use_umma || !umma_fits(m)) {
-        k_gather<<<B, 128, 0, m->stream>>>(x, nullptr, nullptr, B, m->width[0], m->width[m->L], m->H[0], nullptr);
-        cudaError_t e = forward(m, B);
-        if (e != cudaSuccess || B == 0) return e;
-        const long long total = (long long)B * m->width[m->L];
-        k_accumulate<<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, m->stream>>>(
-            y, ldy, m->Z[m->L - 1], B, m->width[m->L], scale, first ? 1 : 0);
-        return cudaGetLastError();
-    }
     cudaError_t e = cudaSuccess;
     if (m->wpk.empty()) {
-        static const cudaError_t attr = cudaFuncSetAttribute(
-            k_umma_layer<kUmmaEpiWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, kUmmaSmem);
+        static const cudaError_t attr = [] {
+            cudaError_t a = cudaFuncSetAttribute(k_umma_layer<kUmmaEpiWarps>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kUmmaSmem);
+            if (a == cudaSuccess)
+                a = cudaFuncSetAttribute(k_umma_mean_layer<kUmmaEpiWarps>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kMeanSmem);
+            return a;
+        }();
         if (attr != cudaSuccess) return attr;
         for (int l = 0; l < m->L; l++) {
             m->kpad.push_back(pad16(m->width[l]));
@@ -1018,7 +1195,27 @@ static cudaError_t forward_infer(pt_mlp *m, int B, const float *x, const bf16 **
             k_pad_bf16<<<grid_for((long long)m->npad[l] * m->kpad[l]), 256, 0, m->stream>>>(
                 m->wb + m->woff[l], m->width[l + 1], m->width[l], m->wpk[l], m->npad[l], m->kpad[l]);
         m->packed_stale = false;
+        e = cudaGetLastError();
     }
+    return e;
+}
+
+// With hidden_only, the tcgen05 path stops after the last hidden layer (H[L-1] holds
+// its activations) and y is not written.
+static cudaError_t forward_infer(pt_mlp *m, int B, const float *x, const bf16 **x0, float *y, long long ldy,
+                                 float scale, bool first, bool hidden_only = false)
+{
+    if (!m->use_umma || !umma_fits(m)) {
+        k_gather<<<B, 128, 0, m->stream>>>(x, nullptr, nullptr, B, m->width[0], m->width[m->L], m->H[0], nullptr);
+        cudaError_t e = forward(m, B);
+        if (e != cudaSuccess || B == 0) return e;
+        const long long total = (long long)B * m->width[m->L];
+        k_accumulate<<<(int)std::min<long long>((total + 255) / 256, 4096), 256, 0, m->stream>>>(
+            y, ldy, m->Z[m->L - 1], B, m->width[m->L], scale, first ? 1 : 0);
+        return cudaGetLastError();
+    }
+    cudaError_t e = umma_prepare(m);
+    if (e != cudaSuccess) return e;
     if (!*x0) {
         k_input_bf16<<<grid_for((long long)B * m->kpad[0] / 8), 256, 0, m->stream>>>(x, B, m->width[0], m->h0p,
                                                                                     m->kpad[0]);
@@ -1027,7 +1224,7 @@ static cudaError_t forward_infer(pt_mlp *m, int B, const float *x, const bf16 **
         *x0 = m->h0p;
     }
     const int tiles = (B + kUmmaM - 1) / kUmmaM;
-    for (int l = 0; l < m->L; l++) {
+    for (int l = 0; l < (hidden_only ? m->L - 1 : m->L); l++) {
         const int Kp = m->kpad[l], Np = m->npad[l];
         const bool last = l + 1 == m->L;
         // one CTA per SM: the full shared-memory request keeps a second one off the SM,
@@ -1052,6 +1249,79 @@ static cudaError_t forward_infer(pt_mlp *m, int B, const float *x, const bf16 **
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+// Whether an ensemble runs its last layers as one GEMM (k_umma_mean_layer): 2 to
+// kMeanMaxMembers members, all on the tcgen05 path, the last layer's input a
+// multiple of 64 wide and its output at most kUmmaMaxN.
+static bool mean_layer_fits(pt_mlp *const *members, int count)
+{
+    if (count < 2 || count > kMeanMaxMembers) return false;
+    for (int j = 0; j < count; j++)
+        if (!members[j]->use_umma || !umma_fits(members[j])) return false;
+    const pt_mlp *m = members[0];
+    return m->L >= 2 && m->width[m->L - 1] % 64 == 0 && pad16(m->width[m->L]) <= kUmmaMaxN;
+}
+
+// The mean of the members' last layers over B rows into y (row stride ldy), after
+// every member's hidden layers have run (H[L-1] of each holds its activations).
+static cudaError_t mean_layer(pt_mlp *const *members, int count, int B, float *y, int ldy, cudaStream_t s)
+{
+    pt_mlp *m = members[0];
+    const int L = m->L, kh = m->width[L - 1], N = m->width[L], np = pad16(N);
+    const size_t need = (size_t)np * kh * count;
+    cudaError_t e = cudaSuccess;
+    if (!m->mean_ptrs) e = dalloc(m, &m->mean_ptrs, 2 * kMeanMaxMembers);
+    if (e == cudaSuccess && !m->bsum) e = dalloc(m, &m->bsum, kUmmaMaxN);
+    if (e == cudaSuccess && m->wcat_elems < need) {
+        e = dalloc(m, &m->wcat, need);
+        if (e == cudaSuccess) m->wcat_elems = need;
+    }
+    if (e != cudaSuccess) return e;
+    void *h[2 * kMeanMaxMembers] = {};
+    for (int j = 0; j < count; j++) {
+        h[j] = members[j]->wpk[L - 1];
+        h[kMeanMaxMembers + j] = members[j]->w + members[j]->boff[L - 1];
+    }
+    e = cudaMemcpyAsync(m->mean_ptrs, h, sizeof(h), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    k_concat_weights<<<grid_for((long long)need), 256, 0, s>>>((const bf16 *const *)m->mean_ptrs, count, np, kh,
+                                                               m->wcat);
+    k_bias_sum<<<1, 256, 0, s>>>((const float *const *)(m->mean_ptrs + kMeanMaxMembers), count, N, m->bsum);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    MeanMaps maps;
+    memset(&maps, 0, sizeof(maps));
+    for (int j = 0; j < count; j++)
+        if (!operand_map(&maps.a[j], members[j]->H[L - 1], B, kh, kh, kUmmaM, true)) return cudaErrorNotSupported;
+    CUtensorMap mw;
+    if (!operand_map(&mw, m->wcat, np, kh * count, (long long)kh * count, np, true)) return cudaErrorNotSupported;
+    const int vec = ldy % 32 == 0 && ldy >= pad32(N) && reinterpret_cast<uintptr_t>(y) % 32 == 0;
+    const int tiles = (B + kUmmaM - 1) / kUmmaM;
+    const int grid = std::max(1, std::min(tiles, sm_count_mlp()));
+    k_umma_mean_layer<kUmmaEpiWarps><<<grid, 32 * (2 + kUmmaEpiWarps), kMeanSmem, s>>>(
+        maps, mw, B, kh, count, np, N, m->bsum, 1.0f / (float)count, y, ldy, vec, m->umma_err);
+    return cudaGetLastError();
+}
+
+// One chunk of B rows of x (device) through every member, their mean into acc (row
+// stride ldacc): the members' hidden layers, then one mean layer when it fits, else
+// each member's last layer accumulating in its epilogue.
+static cudaError_t ensemble_chunk(pt_mlp *const *members, int count, int B, const float *x, float *acc, int ldacc,
+                                  cudaStream_t s)
+{
+    const bool fused = mean_layer_fits(members, count);
+    const bf16 *x0 = nullptr;
+    cudaError_t e = cudaSuccess;
+    for (int j = 0; j < count && e == cudaSuccess; j++) {
+        pt_mlp *q = members[j];
+        const cudaStream_t own = q->stream;
+        q->stream = s;
+        e = forward_infer(q, B, x, &x0, acc, ldacc, 1.0f / (float)count, j == 0, fused);
+        q->stream = own;
+    }
+    if (e != cudaSuccess || !fused || B == 0) return e;
+    return mean_layer(members, count, B, acc, ldacc, s);
 }
 
 // A device wait of the tcgen05 path that gave up: reported once, then cleared.
@@ -1305,14 +1575,7 @@ pt_status pt_mlp_predict_ensemble(pt_mlp *const *members, int count, const float
     for (int s0 = 0; s0 < n && e == cudaSuccess; s0 += chunk) {
         const int B = std::min(chunk, n - s0);
         e = cudaMemcpyAsync(dX, X + (size_t)s0 * din, (size_t)B * din * sizeof(float), cudaMemcpyHostToDevice, s);
-        const bf16 *x0 = nullptr;
-        for (int j = 0; j < count && e == cudaSuccess; j++) {
-            pt_mlp *q = members[j];
-            const cudaStream_t own = q->stream;
-            q->stream = s;
-            e = forward_infer(q, B, dX, &x0, acc, m->ldz, 1.0f / (float)count, j == 0);
-            q->stream = own;
-        }
+        if (e == cudaSuccess) e = ensemble_chunk(members, count, B, dX, acc, m->ldz, s);
         if (e == cudaSuccess)
             e = copy_out(acc, m->ldz, m->Z[m->L - 1], B, dout, Y + (size_t)s0 * dout, cudaMemcpyDeviceToHost, s);
     }
@@ -1347,16 +1610,7 @@ pt_status pt_mlp_predict_ensemble_device(pt_mlp *const *members, int count, cons
     MCK(ensure_zout(m), "inference output");
     for (int s0 = 0; s0 < n; s0 += chunk) {
         const int B = std::min(chunk, n - s0);
-        const bf16 *x0 = nullptr;
-        for (int j = 0; j < count; j++) {
-            pt_mlp *q = members[j];
-            const cudaStream_t own = q->stream;
-            q->stream = s;
-            const cudaError_t e =
-                forward_infer(q, B, X + (size_t)s0 * din, &x0, m->zout, m->ldz, 1.0f / (float)count, j == 0);
-            q->stream = own;
-            MCK(e, "ensemble predict (device)");
-        }
+        MCK(ensemble_chunk(members, count, B, X + (size_t)s0 * din, m->zout, m->ldz, s), "ensemble predict (device)");
         // the mean, from the padded accumulator into y's rows
         MCK(copy_out(m->zout, m->ldz, nullptr, B, dout, Y + (size_t)s0 * dout, cudaMemcpyDeviceToDevice, s),
             "ensemble mean");

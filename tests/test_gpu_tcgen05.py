@@ -79,3 +79,21 @@ def test_tcgen05_ensemble_on_device_buffers_equals_host_path(native_lib):
     torch.cuda.synchronize()
     np.testing.assert_array_equal(yd.cpu().numpy(), y_host)
     s.close()
+
+
+def test_ensemble_mean_layer_equals_the_mean_of_the_members(native_lib):
+    """An ensemble runs its members' last layers as one GEMM over their concatenated
+    activations (k_umma_mean_layer).  Its output equals the mean of the members' own
+    predictions up to FP32 summation order: the hidden layers are the same kernels."""
+    rng = np.random.default_rng(21)
+    s = sg.Surrogate(1_000_000, seed=5, members=4, max_batch=2048)
+    for net in s.nets:
+        p = net.get_params()
+        net.set_params(p + rng.standard_normal(p.shape).astype(np.float32) * 0.05)
+    X = sg.features(sg.sample_scenarios(3000, rng))   # two chunks, the second a partial tile
+    y = s.raw_features(X)
+    each = np.mean([net.predict(X) for net in s.nets], axis=0)
+    s.close()
+    scale = np.abs(each).max()
+    assert np.isfinite(y).all()
+    assert np.abs(y - each).max() <= 1e-5 * scale
