@@ -312,7 +312,16 @@ pt_status pt_mlp_set_tcgen05(pt_mlp *mlp, int enabled);
 void pt_mlp_destroy(pt_mlp *mlp);
 const char *pt_mlp_last_error(const pt_mlp *mlp);
 
+/* Returns the simulation's device memory to the library's pool.  Simulations and
+ * batches take their device memory from one stream-ordered pool per GPU that keeps
+ * what they free, so creating and destroying simulations of similar sizes (replicate
+ * loops, scenario sweeps) reuses it instead of mapping and unmapping it each time. */
 void pt_destroy(pt_sim *sim);
+
+/* Hands the memory the pool of the current GPU keeps, and no simulation uses, back to
+ * the device (cudaMemPoolTrimTo).  Call it before allocating elsewhere what the
+ * library no longer needs. */
+pt_status pt_trim_device_memory(void);
 
 /* Text of the last error on sim (or of the last failed pt_create when sim is NULL). */
 const char *pt_last_error(const pt_sim *sim);

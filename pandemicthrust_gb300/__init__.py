@@ -115,7 +115,8 @@ EXPORTS = [
     "pt_batch_get_person_state", "pt_batch_get_population", "pt_batch_set_timing", "pt_batch_get_stage_ms",
     "pt_batch_transfer_bytes", "pt_batch_destroy", "pt_batch_last_error",
     "pt_set_tuning", "pt_get_tuning", "pt_autotune", "pt_batch_set_tuning", "pt_batch_get_tuning",
-    "pt_batch_autotune", "pt_selftest_bounded_wait", "pt_selftest_errand_lookup", "pt_bucket_table_static",
+    "pt_batch_autotune", "pt_selftest_bounded_wait", "pt_selftest_errand_lookup", "pt_trim_device_memory",
+    "pt_bucket_table_static",
 ]
 
 _lib = None
@@ -161,6 +162,7 @@ def load_library(path=None):
         getattr(lib, pre + "autotune").argtypes = [vp, ctypes.c_int, tp]
     lib.pt_selftest_bounded_wait.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint32)]
     lib.pt_selftest_errand_lookup.argtypes = [ctypes.POINTER(ctypes.c_uint64)]
+    lib.pt_trim_device_memory.argtypes = []
     lib.pt_launch_count.restype = ctypes.c_uint64
     lib.pt_launch_count.argtypes = []
     lib.pt_transfer_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]

@@ -108,6 +108,54 @@ struct pt_batch : Engine {};
 
 // Every host<->device copy of the library goes through these, so the bytes a call
 // moves across PCIe/C2C can be reported (pt_transfer_bytes).
+// Engines take their device memory from one stream-ordered pool per device that keeps
+// the blocks engines free (release threshold at its maximum): creating and destroying
+// engines of similar sizes, as replicate loops and scenario sweeps do, reuses memory
+// instead of mapping and unmapping gigabytes each time.  pt_trim_device_memory hands
+// the unused part back to the device.
+static std::mutex g_pool_mu;
+static std::map<int, cudaMemPool_t> g_pools;
+
+static cudaError_t engine_pool(cudaMemPool_t *out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> g(g_pool_mu);
+    auto it = g_pools.find(dev);
+    if (it != g_pools.end()) {
+        *out = it->second;
+        return cudaSuccess;
+    }
+    cudaMemPoolProps props;
+    memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p = nullptr;
+    e = cudaMemPoolCreate(&p, &props);
+    if (e != cudaSuccess) return e;
+    uint64_t keep = UINT64_MAX;
+    e = cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (e != cudaSuccess) {
+        cudaMemPoolDestroy(p);
+        return e;
+    }
+    g_pools[dev] = p;
+    *out = p;
+    return cudaSuccess;
+}
+
+// Device memory for an engine, ordered on its stream; freed with cudaFreeAsync.
+static cudaError_t engine_alloc(void **ptr, size_t bytes, cudaStream_t st)
+{
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = engine_pool(&pool);
+    if (e != cudaSuccess) return e;
+    return cudaMallocFromPoolAsync(ptr, bytes, pool, st);
+}
+
 static cudaError_t pt_memcpy(const Engine *s, void *dst, const void *src, size_t n, cudaMemcpyKind k, cudaStream_t st)
 {
     if (k == cudaMemcpyHostToDevice) s->h2d_bytes += n;
@@ -145,9 +193,11 @@ Engine::~Engine()
 {
     if (stream) cudaStreamSynchronize(stream);
     if (run_graph) cudaGraphExecDestroy(run_graph);
-    cudaFree(arena_mem);
-    cudaFree(setup_mem);
-    cudaFree(small_mem);
+    // back to the pool, in stream order
+    if (arena_mem) cudaFreeAsync(arena_mem, stream);
+    if (setup_mem) cudaFreeAsync(setup_mem, stream);
+    if (small_mem) cudaFreeAsync(small_mem, stream);
+    if (stream) cudaStreamSynchronize(stream);
     for (auto &e : day_events)
         if (e) cudaEventDestroy(e);
     if (own_stream && stream) cudaStreamDestroy(stream);
@@ -279,7 +329,7 @@ static pt_status engine_setup(Engine *s)
                                round256((size_t)K * sizeof(ptk::InstConst)) + round256((size_t)K * sizeof(ptk::InstState)) +
                                round256((size_t)K * 512 * sizeof(int)) + round256(((size_t)HS + 1) * 4) +
                                round256((size_t)2 * K * sizeof(int));
-    CK(cudaMalloc(&s->small_mem, small_bytes), "cudaMalloc(small)");
+    CK(engine_alloc((void **)&s->small_mem, small_bytes, s->stream), "device memory (small)");
     s->small_bytes = small_bytes;
     Arena a0{s->small_mem, small_bytes, 0};
     d.sc = a0.take<ptk::Scalars>(1);
@@ -293,7 +343,7 @@ static pt_status engine_setup(Engine *s)
     int *d_counts = a0.take<int>((size_t)2 * K);  // adults, persons per instance
     // setup-only block: household types and sizes
     const size_t setup_bytes = round256((size_t)HS) + round256((size_t)HS * 4);
-    CK(cudaMalloc(&s->setup_mem, setup_bytes), "cudaMalloc(setup)");
+    CK(engine_alloc((void **)&s->setup_mem, setup_bytes, s->stream), "device memory (setup)");
     Arena a1{s->setup_mem, setup_bytes, 0};
     uint8_t *types = a1.take<uint8_t>((size_t)HS);
     int32_t *sizes = a1.take<int32_t>((size_t)HS);
@@ -385,7 +435,7 @@ static pt_status engine_setup(Engine *s)
     bytes += round256(2 * n * 4);               // new_list
     bytes += round256((size_t)(nseeds + 1) * 4);  // seeds
     bytes += round256(ntiles * 4);              // tile_inst
-    CK(cudaMalloc(&s->arena_mem, bytes), "cudaMalloc(arena)");
+    CK(engine_alloc((void **)&s->arena_mem, bytes, s->stream), "device memory (arena)");
     s->arena_bytes = bytes;
     Arena a{s->arena_mem, bytes, 0};
     d.state = a.take<uint32_t>(n);
@@ -479,7 +529,7 @@ static pt_status engine_setup(Engine *s)
     int derr = 0;
     CK(pt_memcpy(s, &derr, &d.sc->error, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "error flag");
     CK(cudaStreamSynchronize(s->stream), "setup sync");
-    cudaFree(s->setup_mem);
+    cudaFreeAsync(s->setup_mem, s->stream);
     s->setup_mem = nullptr;
     if (derr) return fail(s, PT_ERR_TIMEOUT, "a device-side wait gave up during setup");
     pt_status st = engine_reset(s);
@@ -1226,6 +1276,15 @@ pt_status pt_selftest_errand_lookup(uint64_t counts[4])
     cudaFree(d);
     if (e != cudaSuccess) return cuda_fail(nullptr, e, "errand self-test");
     for (int i = 0; i < 4; i++) counts[i] = h[i];
+    return PT_OK;
+}
+
+pt_status pt_trim_device_memory(void)
+{
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = engine_pool(&pool);
+    if (e == cudaSuccess) e = cudaMemPoolTrimTo(pool, 0);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "trim device memory");
     return PT_OK;
 }
 
