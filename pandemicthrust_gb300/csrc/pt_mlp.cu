@@ -948,7 +948,9 @@ struct pt_mlp {
     std::vector<int> kpad, npad;
     bf16 *h0p = nullptr;
     int *umma_err = nullptr;
-    // inference output: the last layer's outputs, rows padded to a multiple of 32
+    // inference input (FP32 rows copied from the host) and output (the last layer's
+    // outputs, rows padded to a multiple of 32), max_batch rows each
+    float *xin = nullptr;
     float *zout = nullptr;
     int ldz = 0;
     // the ensemble mean layer (held by an ensemble's first network): the members' last
@@ -1147,10 +1149,12 @@ static cudaError_t copy_out(const float *src, int lds, float *staging, int rows,
     return e;
 }
 
-// The padded inference output buffer of a network (max_batch x ldz).
+// The inference input and padded output buffers of a network, kept between calls.
 static cudaError_t ensure_zout(pt_mlp *m)
 {
     if (m->zout) return cudaSuccess;
+    cudaError_t e = dalloc(m, &m->xin, (size_t)m->max_batch * m->width[0]);
+    if (e != cudaSuccess) return e;
     m->ldz = pad32(m->width[m->L]);
     return dalloc(m, &m->zout, (size_t)m->max_batch * m->ldz);
 }
@@ -1518,10 +1522,9 @@ pt_status pt_mlp_predict(pt_mlp *m, const float *X, int n, float *Y)
 {
     if (!m || !X || !Y || n < 0) return PT_ERR_ARG;
     const int din = m->width[0], dout = m->width[m->L];
-    float *dX = nullptr;
     const int chunk = m->max_batch;
-    MCK(ensure_zout(m), "inference output");
-    MCK(cudaMalloc(&dX, (size_t)std::max(1, std::min(n, chunk)) * din * sizeof(float)), "batch");
+    MCK(ensure_zout(m), "inference buffers");
+    float *dX = m->xin;
     cudaError_t e = cudaSuccess;
     for (int s0 = 0; s0 < n && e == cudaSuccess; s0 += chunk) {
         const int B = std::min(chunk, n - s0);
@@ -1535,7 +1538,6 @@ pt_status pt_mlp_predict(pt_mlp *m, const float *X, int n, float *Y)
                      m->stream);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
-    cudaFree(dX);
     MCK(e, "predict");
     return umma_check(m);
 }
@@ -1567,10 +1569,8 @@ pt_status pt_mlp_predict_ensemble(pt_mlp *const *members, int count, const float
     for (int j = 1; j < count; j++)
         if (members[j]->stream != s) MCK(cudaStreamSynchronize(members[j]->stream), "ensemble member stream");
     // the members' mean accumulates in the first member's padded output buffer
-    MCK(ensure_zout(m), "inference output");
-    float *dX = nullptr, *acc = m->zout;
-    const size_t rows = (size_t)std::max(1, std::min(n, chunk));
-    MCK(cudaMalloc(&dX, rows * din * sizeof(float)), "batch");
+    MCK(ensure_zout(m), "inference buffers");
+    float *dX = m->xin, *acc = m->zout;   // chunk <= m->max_batch rows
     cudaError_t e = cudaSuccess;
     for (int s0 = 0; s0 < n && e == cudaSuccess; s0 += chunk) {
         const int B = std::min(chunk, n - s0);
@@ -1580,7 +1580,6 @@ pt_status pt_mlp_predict_ensemble(pt_mlp *const *members, int count, const float
             e = copy_out(acc, m->ldz, m->Z[m->L - 1], B, dout, Y + (size_t)s0 * dout, cudaMemcpyDeviceToHost, s);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    cudaFree(dX);
     MCK(e, "ensemble predict");
     for (int j = 0; j < count; j++) {
         const pt_status st = umma_check(members[j]);
