@@ -168,6 +168,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def apply_tuning(engine, spec):
+    """Launch shapes of an engine: its tuner's choice ("auto"), the library's defaults
+    ("default"), or the defaults with name=value overrides ("sched_tf=1,infect_coop=1").
+    Every choice gives identical results.  Returns the shapes in use."""
+    if spec == "auto":
+        return engine.autotune()
+    if spec != "default":
+        t = engine.tuning()
+        for item in spec.split(","):
+            name, _, value = item.partition("=")
+            if name.strip() not in t:
+                raise SystemExit("--tuning: unknown launch shape %r (known: %s)" % (name, ", ".join(t)))
+            t[name.strip()] = int(value)
+        engine.set_tuning(t)
+    return engine.tuning()
+
+
 def reduce_replicas(ms, person_days, device):
     """Whole-job figures over replica ranks: total person-days and the slowest rank's
     time (max over ranks).  One independent simulation per rank, no data exchange."""
@@ -415,7 +432,7 @@ def run_batched(args, pt, torch, stream, local):
     b = pt.PandemicBatch(params, seeds, stream=sp)
     b.setup()
     # launch shapes for this batch (part of the warm-up)
-    tuning = b.autotune() if args.tuning == "auto" else b.tuning()
+    tuning = apply_tuning(b, args.tuning)
     K, persons, padded = b.size()
     sizes = [b.info(k)["number_people"] for k in range(K)]
     for _ in range(args.batch_warmup):
@@ -467,8 +484,7 @@ def run_batched(args, pt, torch, stream, local):
     e0.record(stream)
     b2 = pt.PandemicBatch(params, seeds, stream=sp)
     b2.setup()
-    if args.tuning == "auto":
-        b2.autotune()   # the shapes chosen above for this batch size (cached: no timing runs)
+    apply_tuning(b2, args.tuning)   # auto: the shapes chosen above for this size (cached: no timing runs)
     b2.run()
     b2.final_gen_counts()
     e2e_pd = sum(n * int(d) for n, d in zip(sizes, b2.days_run()))
@@ -667,8 +683,9 @@ def main():
     ap.add_argument("--search-judge", type=int, default=4,
                     help="intervention search at 50M: top-1%% scenarios re-simulated (32 replicates each; 0: skip)")
     ap.add_argument("--only-surrogate", action="store_true", help="run the surrogate section alone")
-    ap.add_argument("--tuning", default="auto", choices=["auto", "default"],
-                    help="launch shapes: chosen by pt_autotune, or the library's defaults (profiling captures)")
+    ap.add_argument("--tuning", default="auto",
+                    help="launch shapes: auto (pt_autotune), default (the library's), or name=value pairs, e.g. "
+                         "sched_tf=1,infect_coop=1 (profiling captures of tuned shapes without the tuner's runs)")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="population scale (profiling captures only; the bench line is for 1.0)")
     args = ap.parse_args()
@@ -703,7 +720,7 @@ def main():
     Bc_wd = 2 * (L - info["type_offset"][8])
     Bc_we = 10 * (L - info["type_offset"][9])
     # launch shapes (untimed, before the warm-up)
-    tuning = sim.autotune() if args.tuning == "auto" else sim.tuning()
+    tuning = apply_tuning(sim, args.tuning)
 
     # warm-up steps (untimed)
     for _ in range(args.warmup):
@@ -798,8 +815,7 @@ def main():
         for _ in range(args.e2e_steps):
             s2 = pt.PandemicSim(params, seed, stream=ctypes.c_void_p(stream.cuda_stream))
             s2.setupSim()
-            if args.tuning == "auto":
-                s2.autotune()   # the shapes chosen above for this size (cached: no timing runs)
+            apply_tuning(s2, args.tuning)   # auto: the shapes chosen above for this size (cached: no timing runs)
             c2, i2 = s2.runToCompletion()
             s2.final_gen_counts()
             e2e_days += len(i2)
