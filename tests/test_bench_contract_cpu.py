@@ -4,6 +4,8 @@ import os
 import subprocess
 import sys
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -27,6 +29,7 @@ def test_reference_arm_prints_one_contract_line():
 def test_parity_helpers_flag_a_planted_difference():
     # the comparisons bench.py reports: equal records pass, one changed field fails
     sys.path.insert(0, ROOT)
+    sys.path.insert(0, ROOT)
     import bench
     import numpy as np
     rows = [{"rc": 0, "counts": list(range(16)), "infected": 5, "rand_offset": 100 + d} for d in range(3)]
@@ -42,3 +45,31 @@ def test_parity_helpers_flag_a_planted_difference():
     state2["gen_s"][3] ^= 1
     bad = bench.parity_vs_oracle(rec, {"rows": rows, "digests": bench.state_digests(state2)})
     assert bad["mismatches"] == ["final gen_s"]
+
+
+def test_tuning_spec_sets_named_launch_shapes_and_rejects_unknown_ones():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    class Engine:
+        def __init__(self):
+            self.t = {"infect_coop": 0, "sched_tf": 0, "radix_threads": 256}
+            self.tuned = False
+
+        def tuning(self):
+            return dict(self.t)
+
+        def set_tuning(self, t):
+            self.t = dict(t)
+
+        def autotune(self):
+            self.tuned = True
+            return dict(self.t)
+
+    e = Engine()
+    assert bench.apply_tuning(e, "sched_tf=1,infect_coop=1") == {"infect_coop": 1, "sched_tf": 1, "radix_threads": 256}
+    assert not e.tuned
+    bench.apply_tuning(e, "auto")
+    assert e.tuned
+    with pytest.raises(SystemExit):
+        bench.apply_tuning(Engine(), "no_such_shape=3")
