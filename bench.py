@@ -422,6 +422,36 @@ def run_reference(args, world, rank):
     return 0
 
 
+def run_plain_l_eq_p(pt, torch, stream, tuning, steps=2):
+    """The same 50M-person population with one location per household unit
+    (location_scaling = people_scaling: 271,872 locations instead of 2.72M), the
+    thesis-style shape: fewer, larger buckets.  Same launch shapes as the main run;
+    device time of `steps` 100-day runs after one warm-up run."""
+    params = dict(PARAMS, location_scaling=PARAMS["people_scaling"])
+    sim = pt.PandemicSim(params, SEED, stream=ctypes.c_void_p(stream.cuda_stream))
+    sim.setupSim()
+    sim.set_tuning(tuning)
+    info = sim.info()
+    sim.reset_epidemic()
+    sim.runToCompletion()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    days = 0
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        sim.reset_epidemic()
+        _, inf = sim.runToCompletion()
+        days += len(inf)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    sim.close()
+    N = info["number_people"]
+    return {"workload": "plain_50M_persons_l_eq_p_100_days", "persons": N, "locations": info["number_workplaces"],
+            "value": N * days / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / steps, "steps": steps,
+            "note": "location_scaling = people_scaling; the headline uses 10x as many locations"}
+
+
 def run_batched(args, pt, torch, stream, local):
     """The batched workload (256 uneven instances x 100 days, one batch) and the same
     instances run one after another through the plain path, both timed with CUDA
@@ -686,6 +716,7 @@ def main():
     ap.add_argument("--tuning", default="auto",
                     help="launch shapes: auto (pt_autotune), default (the library's), or name=value pairs, e.g. "
                          "sched_tf=1,infect_coop=1 (profiling captures of tuned shapes without the tuner's runs)")
+    ap.add_argument("--no-lp", action="store_true", help="skip the location_scaling = people_scaling run")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="population scale (profiling captures only; the bench line is for 1.0)")
     args = ap.parse_args()
@@ -832,6 +863,10 @@ def main():
     else:
         sim.close()
 
+    plain_lp = None
+    if world == 1 and args.scale == 1.0 and not args.no_lp:
+        plain_lp = run_plain_l_eq_p(pt, torch, stream, tuning)
+
     batched = None
     if args.batch_instances > 0 and world == 1:
         batched = run_batched(args, pt, torch, stream, local)
@@ -877,6 +912,7 @@ def main():
             "buckets_materialised_fraction": round(mat_frac, 4),
             "cpu_baseline": cpu,
             "clocks": clocks,
+            "plain_l_eq_p": plain_lp,
             "batched": batched,
             "surrogate": surrogate,
         }
