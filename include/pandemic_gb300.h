@@ -188,7 +188,8 @@ pt_status pt_get_day_stage_ms(pt_sim *sim, int day, float ms[8]);
 typedef struct pt_tuning {
     int infect_coop;            /* 0: one thread per infector; 1: eight lanes per infector */
     int infect_blocks_per_sm;   /* infection grid, 256-thread blocks per SM: 1..32 */
-    int radix_blocks_per_sm;    /* persistent blocks of a day's radix pass per SM: 1..3 */
+    int radix_blocks_per_sm;    /* persistent blocks of a day's radix pass per SM: 1..4
+                                   (3 at 80 registers a thread, 4 at 64) */
     int sched_tf;               /* the schedule kernel's Threefry arithmetic (same results):
                                    0 integer adds and funnel shifts; 1 the 64-bit adds as
                                    multiply-adds with carry; 2 also the rotations as wide

@@ -371,8 +371,8 @@ __device__ __forceinline__ uint32_t pack_rank(unsigned d, unsigned rank, unsigne
 // segments' tiles are numbered consecutively (segment k owns tiles
 // [tile_prefix[k], tile_prefix[k + 1])), and the look-back of a segment's first tile
 // starts from zero.  Unsegmented sorts are one segment [0, E).
-template <int MODE, int THREADS>
-__global__ void __launch_bounds__(THREADS, THREADS == 256 ? 3 : 2) k_radix_pass(const uint32_t *__restrict__ keys_in,
+template <int MODE, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_radix_pass(const uint32_t *__restrict__ keys_in,
                                                                  const uint32_t *__restrict__ vals_in,
                                                                  uint32_t *__restrict__ keys_out,
                                                                  uint32_t *__restrict__ vals_out, int E_arg,
@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(THREADS, THREADS == 256 ? 3 : 2) k_radix_pass(
     __shared__ int s_seg[8];
     __shared__ unsigned s_epoch;
     __shared__ int s_hist[WARPS][256];
-    __shared__ int s_base[256];   // global position of the tile's first entry of each digit
+    __shared__ int s_base[256];   // global position of digit d's entries, less its tile-local start
     __shared__ int s_toff[256];   // tile-local position of each digit's first entry
     __shared__ uint32_t s_key[kRadixTile];
     __shared__ uint32_t s_val[kRadixTile];
@@ -453,7 +453,13 @@ __global__ void __launch_bounds__(THREADS, THREADS == 256 ? 3 : 2) k_radix_pass(
         if (tile >= tiles) break;
         const int seg = s_seg[0], stile = s_seg[1], sbase = s_seg[2], scount = s_seg[3];
         const bool dense = s_seg[4] != 0;
-        for (int i = threadIdx.x; i < WARPS * 256; i += THREADS) (&s_hist[0][0])[i] = 0;
+        // the peer words of phase A alias the first WARPS * 256 words of s_key, which
+        // phase B only writes after the barrier that ends phase A
+        unsigned *const s_peer = s_key + warp * 256;
+        for (int i = threadIdx.x; i < WARPS * 256; i += THREADS) {
+            (&s_hist[0][0])[i] = 0;
+            s_key[i] = 0u;
+        }
         __syncthreads();
         const int base = stile * kRadixTile + warp * WARP_ITEMS + lane;  // index within the segment
         const bool full = (stile + 1) * kRadixTile <= scount;
@@ -487,24 +493,49 @@ __global__ void __launch_bounds__(THREADS, THREADS == 256 ? 3 : 2) k_radix_pass(
                 }
             }
         }
-        // phase A: rank within the warp round, per-warp digit counts
+        // phase A: rank within the warp round, per-warp digit counts.  The lanes holding
+        // the same digit come from one ballot per digit bit for narrow digits, and for
+        // wider ones from a shared word per digit that each lane ORs its bit into (the
+        // leader clears it again); both give the same set.
+        if (nbits <= 4) {
 #pragma unroll
-        for (int j = 0; j < ITEMS; j++) {
-            const int i = base + 32 * j;
-            bool ok = (full || i < scount) && val[j] != kDropped;
-            if ((MODE == kRadixFirst || MODE == kRadixOnly) && mark && ok)
-                ok = (mark[key[j] >> 5] >> (key[j] & 31u)) & 1u;
-            const unsigned d = (key[j] >> shift) & 255u;
-            const unsigned peers = digit_peers(d, nbits, __ballot_sync(0xffffffffu, ok));
-            const unsigned rank = __popc(peers & lt), cnt = __popc(peers);
-            if (ok && rank == 0) s_hist[warp][d] += cnt;
-            info[j] = pack_rank(d, rank, cnt, ok);
+            for (int j = 0; j < ITEMS; j++) {
+                const int i = base + 32 * j;
+                bool ok = (full || i < scount) && val[j] != kDropped;
+                if ((MODE == kRadixFirst || MODE == kRadixOnly) && mark && ok)
+                    ok = (mark[key[j] >> 5] >> (key[j] & 31u)) & 1u;
+                const unsigned d = (key[j] >> shift) & 255u;
+                const unsigned peers = digit_peers(d, nbits, __ballot_sync(0xffffffffu, ok));
+                const unsigned rank = __popc(peers & lt), cnt = __popc(peers);
+                if (ok && rank == 0) s_hist[warp][d] += cnt;
+                info[j] = pack_rank(d, rank, cnt, ok);
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < ITEMS; j++) {
+                const int i = base + 32 * j;
+                bool ok = (full || i < scount) && val[j] != kDropped;
+                if ((MODE == kRadixFirst || MODE == kRadixOnly) && mark && ok)
+                    ok = (mark[key[j] >> 5] >> (key[j] & 31u)) & 1u;
+                const unsigned d = (key[j] >> shift) & 255u;
+                if (ok) atomicOr(&s_peer[d], 1u << lane);
+                __syncwarp();
+                const unsigned peers = ok ? s_peer[d] : 0u;
+                __syncwarp();
+                const unsigned rank = __popc(peers & lt), cnt = __popc(peers);
+                if (ok && rank == 0) {
+                    s_peer[d] = 0u;
+                    s_hist[warp][d] += cnt;
+                }
+                __syncwarp();
+                info[j] = pack_rank(d, rank, cnt, ok);
+            }
         }
         __syncthreads();
         {
             // thread d < 256: exclusive bases of the warps for digit d, then the look-back
             const int d = threadIdx.x;
-            int run = 0;
+            int run = 0, gbase = 0;
             if (d < 256) {
 #pragma unroll
                 for (int w = 0; w < WARPS; w++) {
@@ -537,12 +568,15 @@ __global__ void __launch_bounds__(THREADS, THREADS == 256 ? 3 : 2) k_radix_pass(
                     }
                     st[(size_t)tile * 256 + d] = lb_word(epoch, 2, (unsigned)(excl + run));
                 }
-                s_base[d] = sbase + digit_base[((size_t)seg * passes + pass) * 256 + d] + excl;
+                gbase = sbase + digit_base[((size_t)seg * passes + pass) * 256 + d] + excl;
             }
             // tile-local start of digit d (entries of the tile ordered by digit)
             int tile_total;
             const int toff = block_exclusive_scan<THREADS, int>(run, tile_total);
-            if (d < 256) s_toff[d] = toff;
+            if (d < 256) {
+                s_toff[d] = toff;
+                s_base[d] = gbase - toff;
+            }
             if (d == 0) s_tile = tile_total;  // reuse: valid entries of this tile
         }
         __syncthreads();
@@ -568,7 +602,7 @@ __global__ void __launch_bounds__(THREADS, THREADS == 256 ? 3 : 2) k_radix_pass(
         for (int i = threadIdx.x; i < valid; i += THREADS) {
             const uint32_t k = s_key[i];
             const unsigned d = (k >> shift) & 255u;
-            const int pos = s_base[d] + (i - s_toff[d]);
+            const int pos = s_base[d] + i;
             if (MODE == kRadixFirst || MODE == kRadixMiddle || keys_out) keys_out[pos] = k;
             vals_out[pos] = s_val[i];
         }
@@ -601,8 +635,12 @@ cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
     const int bits = key_bits(r.buckets);
     const int tiles = std::max(1, div_up(r.E, kRadixTile));
     const bool wide = r.threads == 512;   // 512 threads x 8 entries per tile, at most 2 blocks per SM
-    const int bps = std::max(1, std::min(wide ? 2 : 3, r.blocks_per_sm));
+    // 256 threads: 3 blocks per SM at 80 registers, or 4 at 64 (the passes with explicit
+    // values only; the implicit-value first pass keeps 3)
+    const int bps = std::max(1, std::min(wide ? 2 : 4, r.blocks_per_sm));
+    const bool four = !wide && bps == 4;
     const int grid = std::max(1, std::min(tiles, bps * sm_count()));  // persistent blocks
+    const int grid3 = std::max(1, std::min(tiles, std::min(bps, 3) * sm_count()));
     const uint32_t *kin = r.keys;
     const uint32_t *vin = r.vals;   // nullptr: implicit values (entry index -> person)
     const bool implicit = r.vals == nullptr;
@@ -620,17 +658,21 @@ cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s)
 #define PT_RADIX_ARGS kin, vin, kout, vout, r.E, cnt, mk, p, P, nbits, r.N, r.person_mode, r.digit_base, r.seg, r.status, \
                       r.ctl, r.error, r.skip
         if (P == 1 && implicit)
-            k_radix_pass<kRadixOnly, kRadixThreads><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+            k_radix_pass<kRadixOnly, kRadixThreads, 3><<<grid3, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
         else if (p == 0 && implicit)
-            k_radix_pass<kRadixFirst, kRadixThreads><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+            k_radix_pass<kRadixFirst, kRadixThreads, 3><<<grid3, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
         else if (p == P - 1 && wide)
-            k_radix_pass<kRadixLast, 512><<<grid, 512, 0, s>>>(PT_RADIX_ARGS);
+            k_radix_pass<kRadixLast, 512, 2><<<grid, 512, 0, s>>>(PT_RADIX_ARGS);
+        else if (p == P - 1 && four)
+            k_radix_pass<kRadixLast, kRadixThreads, 4><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
         else if (p == P - 1)
-            k_radix_pass<kRadixLast, kRadixThreads><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+            k_radix_pass<kRadixLast, kRadixThreads, 3><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
         else if (wide)
-            k_radix_pass<kRadixMiddle, 512><<<grid, 512, 0, s>>>(PT_RADIX_ARGS);
+            k_radix_pass<kRadixMiddle, 512, 2><<<grid, 512, 0, s>>>(PT_RADIX_ARGS);
+        else if (four)
+            k_radix_pass<kRadixMiddle, kRadixThreads, 4><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
         else
-            k_radix_pass<kRadixMiddle, kRadixThreads><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
+            k_radix_pass<kRadixMiddle, kRadixThreads, 3><<<grid, kRadixThreads, 0, s>>>(PT_RADIX_ARGS);
 #undef PT_RADIX_ARGS
         count_launch();
         e = cudaGetLastError();

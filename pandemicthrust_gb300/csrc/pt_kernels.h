@@ -89,7 +89,7 @@ struct Tuning {
     int infect_coop = 0;            // 1: warp-cooperative contacts (8 lanes per infector)
     int infect_blocks_per_sm = 8;   // infection grid: 256-thread blocks per SM (twice as
                                     // many 128-thread blocks for the thread-per-infector kernels)
-    int radix_blocks_per_sm = 3;    // persistent blocks of a day's radix pass per SM (1..3)
+    int radix_blocks_per_sm = 4;    // persistent blocks of a day's radix pass per SM (1..4)
     int sched_tf = 0;               // schedule kernel's Threefry arithmetic: 0 ALU adds and
                                     // shifts, 1 multiply-add adds, 2 also multiply rotations
     int dense_level = 0;            // when a day's sort reads the schedule keys directly:
@@ -212,9 +212,9 @@ struct RadixArgs {
     int *ctl;                     // ticket, finished, epoch
     int *error;
     const int *skip;
-    int blocks_per_sm = 3;        // persistent blocks per SM (1..3, the kernel's occupancy bound)
+    int blocks_per_sm = 3;        // persistent blocks per SM (1..4; 4 only for 256 threads)
     int threads = 256;            // threads per block of the explicit-value passes: 256 (16 entries
-                                  // each, up to 3 blocks per SM) or 512 (8 each, up to 2 blocks)
+                                  // each, up to 4 blocks per SM) or 512 (8 each, up to 2 blocks)
 };
 int radix_passes(int buckets);
 cudaError_t launch_radix_sort(const RadixArgs &r, cudaStream_t s);

@@ -897,7 +897,7 @@ static pt_tuning to_public(const ptk::Tuning &t)
 static pt_status engine_set_tuning(Engine *s, const pt_tuning *t)
 {
     if (!t || (t->infect_coop != 0 && t->infect_coop != 1) || t->infect_blocks_per_sm < 1 ||
-        t->infect_blocks_per_sm > 32 || t->radix_blocks_per_sm < 1 || t->radix_blocks_per_sm > 3 ||
+        t->infect_blocks_per_sm > 32 || t->radix_blocks_per_sm < 1 || t->radix_blocks_per_sm > 4 ||
         t->sched_tf < 0 || t->sched_tf > 2 || t->dense_level < 0 || t->dense_level > 3 ||
         (t->radix_threads != 256 && t->radix_threads != 512) ||
         (t->radix_threads == 512 && t->radix_blocks_per_sm > 2))
@@ -954,7 +954,7 @@ static pt_status engine_autotune(Engine *s, int days, pt_tuning *chosen)
     // warp-cooperative kernel: 6 resident 256-thread blocks per SM at 40 registers
     const Cand infect[] = {{0, 8}, {0, 4}, {1, 6}, {1, 12}, {1, 3}, {0, 16}};
     // radix passes: (blocks per SM, threads per block)
-    const int radix[] = {3, 2, 2};
+    const int radix[] = {3, 4, 2};
     const int radix_threads[] = {256, 256, 512};
     const int tfs[] = {0, 1, 2};
     const int runs = (int)(sizeof(infect) / sizeof(infect[0]));

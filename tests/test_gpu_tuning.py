@@ -22,7 +22,7 @@ SHAPES = [dict(infect_coop=0, infect_blocks_per_sm=8, radix_blocks_per_sm=3, sch
                radix_threads=512),
           dict(infect_coop=0, infect_blocks_per_sm=1, radix_blocks_per_sm=1, sched_tf=2, dense_level=3,
                radix_threads=256),
-          dict(infect_coop=1, infect_blocks_per_sm=32, radix_blocks_per_sm=3, sched_tf=1, dense_level=1,
+          dict(infect_coop=1, infect_blocks_per_sm=32, radix_blocks_per_sm=4, sched_tf=1, dense_level=1,
                radix_threads=256)]
 
 FIELDS = ("status_p", "status_s", "day_p", "day_s", "gen_p", "gen_s")
@@ -82,7 +82,7 @@ def test_batch_shapes_and_autotune_are_identical(native_lib):
         b.setup()
         if shape == "auto":
             chosen = b.autotune(days=12)
-            assert chosen["infect_coop"] in (0, 1) and 1 <= chosen["radix_blocks_per_sm"] <= 3
+            assert chosen["infect_coop"] in (0, 1) and 1 <= chosen["radix_blocks_per_sm"] <= 4
             assert b.tuning() == chosen
         else:
             b.set_tuning(shape)
@@ -118,7 +118,7 @@ def test_bad_shapes_are_rejected(native_lib):
     sim = pt.PandemicSim(make_params(max_days=2, people_scaling=0.001, location_scaling=0.001), 1)
     ok = dict(infect_coop=0, infect_blocks_per_sm=4, radix_blocks_per_sm=1, sched_tf=0, dense_level=0,
               radix_threads=256)
-    for bad in (dict(ok, infect_coop=2), dict(ok, infect_blocks_per_sm=0), dict(ok, radix_blocks_per_sm=4),
+    for bad in (dict(ok, infect_coop=2), dict(ok, infect_blocks_per_sm=0), dict(ok, radix_blocks_per_sm=5),
                 dict(ok, sched_tf=3), dict(ok, dense_level=4), dict(ok, radix_threads=384),
                 dict(ok, radix_threads=512, radix_blocks_per_sm=3)):
         with pytest.raises(pt.PtError):
