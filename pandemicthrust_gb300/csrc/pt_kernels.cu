@@ -351,12 +351,27 @@ __device__ __forceinline__ unsigned digit_peers(unsigned d, int nbits, unsigned 
     return peers;
 }
 
-// Per-item rank record kept between the two phases of a pass:
-// bits 0-7 digit, 8-12 rank among same-digit lanes of the warp round, 13-18 their
-// count, bit 19 valid.
-__device__ __forceinline__ uint32_t pack_rank(unsigned d, unsigned rank, unsigned cnt, bool ok)
+// Per-item record kept between the two phases of a pass: bits 0-7 digit, 8-16 the
+// entry's place among the warp's entries of that digit (earlier rounds, then lanes),
+// bit 17 valid.
+__device__ __forceinline__ uint32_t pack_place(unsigned d, unsigned place, bool ok)
 {
-    return d | (rank << 8) | (cnt << 13) | ((unsigned)ok << 19);
+    return d | (place << 8) | ((unsigned)ok << 17);
+}
+
+// The warp's entries of digit d before this round (s_hist[warp][d]) for every lane of
+// the round: the lowest lane of each digit group advances the count and broadcasts the
+// old value to its group.  Rounds are separated by __syncwarp, so each sees the last.
+__device__ __forceinline__ unsigned warp_digit_before(int *hist_d, unsigned peers, unsigned rank, unsigned cnt,
+                                                      bool ok, int lane)
+{
+    int before = 0;
+    if (ok && rank == 0) {
+        before = *hist_d;
+        *hist_d = before + (int)cnt;
+    }
+    before = __shfl_sync(0xffffffffu, before, ok ? __ffs(peers) - 1 : lane);
+    return (unsigned)before;
 }
 
 // One stable radix pass over 8 bits of the keys.  FILTER (first pass only) drops
@@ -393,7 +408,6 @@ __global__ void __launch_bounds__(THREADS, MINB) k_radix_pass(const uint32_t *__
     __shared__ unsigned s_epoch;
     __shared__ int s_hist[WARPS][256];
     __shared__ int s_base[256];   // global position of digit d's entries, less its tile-local start
-    __shared__ int s_toff[256];   // tile-local position of each digit's first entry
     __shared__ uint32_t s_key[kRadixTile];
     __shared__ uint32_t s_val[kRadixTile];
     const int shift = 8 * pass;
@@ -507,8 +521,9 @@ __global__ void __launch_bounds__(THREADS, MINB) k_radix_pass(const uint32_t *__
                 const unsigned d = (key[j] >> shift) & 255u;
                 const unsigned peers = digit_peers(d, nbits, __ballot_sync(0xffffffffu, ok));
                 const unsigned rank = __popc(peers & lt), cnt = __popc(peers);
-                if (ok && rank == 0) s_hist[warp][d] += cnt;
-                info[j] = pack_rank(d, rank, cnt, ok);
+                const unsigned before = warp_digit_before(&s_hist[warp][d], peers, rank, cnt, ok, lane);
+                __syncwarp();
+                info[j] = pack_place(d, before + rank, ok);
             }
         } else {
 #pragma unroll
@@ -523,12 +538,10 @@ __global__ void __launch_bounds__(THREADS, MINB) k_radix_pass(const uint32_t *__
                 const unsigned peers = ok ? s_peer[d] : 0u;
                 __syncwarp();
                 const unsigned rank = __popc(peers & lt), cnt = __popc(peers);
-                if (ok && rank == 0) {
-                    s_peer[d] = 0u;
-                    s_hist[warp][d] += cnt;
-                }
+                if (ok && rank == 0) s_peer[d] = 0u;
+                const unsigned before = warp_digit_before(&s_hist[warp][d], peers, rank, cnt, ok, lane);
                 __syncwarp();
-                info[j] = pack_rank(d, rank, cnt, ok);
+                info[j] = pack_place(d, before + rank, ok);
             }
         }
         __syncthreads();
@@ -574,27 +587,24 @@ __global__ void __launch_bounds__(THREADS, MINB) k_radix_pass(const uint32_t *__
             int tile_total;
             const int toff = block_exclusive_scan<THREADS, int>(run, tile_total);
             if (d < 256) {
-                s_toff[d] = toff;
                 s_base[d] = gbase - toff;
+                // each warp's first place of digit d in the tile's digit order
+#pragma unroll
+                for (int w = 0; w < WARPS; w++) s_hist[w][d] += toff;
             }
             if (d == 0) s_tile = tile_total;  // reuse: valid entries of this tile
         }
         __syncthreads();
-        // phase B: place each entry in shared memory in digit order (stable) ...
+        // phase B: place each entry in shared memory in digit order (stable): the warp's
+        // first place of its digit plus its place among the warp's entries of that digit ...
 #pragma unroll
         for (int j = 0; j < ITEMS; j++) {
             const uint32_t r = info[j];
-            const bool ok = (r >> 19) & 1u;
-            const unsigned d = r & 255u, rank = (r >> 8) & 31u, cnt = (r >> 13) & 63u;
-            const int wbase = ok ? s_hist[warp][d] : 0;
-            __syncwarp();
-            if (ok) {
-                const int lpos = s_toff[d] + wbase + (int)rank;
+            if ((r >> 17) & 1u) {
+                const int lpos = s_hist[warp][r & 255u] + (int)((r >> 8) & 511u);
                 s_key[lpos] = key[j];
                 s_val[lpos] = val[j];
-                if (rank == 0) s_hist[warp][d] = wbase + (int)cnt;
             }
-            __syncwarp();
         }
         __syncthreads();
         // ... then write each digit's run with consecutive threads (coalesced)
