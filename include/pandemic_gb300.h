@@ -265,10 +265,11 @@ pt_status pt_transfer_bytes(const pt_sim *sim, uint64_t *h2d, uint64_t *d2h);
  * n <= PT_STATIC_TABLE_MAX_ENTRIES and buckets <= PT_STATIC_TABLE_MAX_BUCKETS, else
  * PT_ERR_ARG; a key outside [0, buckets) also gives PT_ERR_ARG.  Work runs on
  * cuda_stream (NULL: the default stream); the call synchronises that stream and
- * returns once the table is complete.  The first call on a device looks up the
- * scratch's device address; make that first call before any stream capture, and
- * make it at initialisation when a memory pool will later claim the device's
- * budget.  The address is kept: do not use the library across a cudaDeviceReset.
+ * returns once the table is complete, so it cannot be captured into a CUDA graph.
+ * The first call on a device (or any kernel of this library) commits the scratch
+ * and looks up its device address; make one call at initialisation when a memory
+ * pool will later claim the device's budget.  The address is kept: do not use the
+ * library across a cudaDeviceReset.
  * All calls share one scratch area, so calls that overlap on the GPU race with each
  * other: do not overlap them. */
 pt_status pt_bucket_table_static(const int32_t *keys, int n, int buckets, int32_t *offsets,
