@@ -906,88 +906,33 @@ __device__ __forceinline__ void tile_begin(const LookBack &lb, const InstConst *
 // The sweep: kernel_countInfectedStatusAndRecover (PandemicSim.cu:2097-2192), the
 // copy_if of the infected (:2207-2224) and runToCompletion's day bookkeeping
 // (:891-937) in three launches over every instance:
-//   count  one person tile per block: recover, count the instance's 16 status bins,
-//          and record each thread's infected persons as a 16-bit mask and the
-//          tile's infected count.  Thread t of a tile holds persons
-//          (r * 256 + t) * 4 + j, rounds r = 0..3, items j = 0..3; mask bit 4r + j.
+//   count  four person tiles per block (one for small runs): recover, count the
+//          instances' 16 status bins (reduced once per block and instance), and
+//          record each thread's infected persons as a 16-bit mask and each tile's
+//          infected count.  Thread t of a tile holds persons (r * 256 + t) * 4 + j,
+//          rounds r = 0..3, items j = 0..3; mask bit 4r + j.
 //   scan   one block: exclusive scan of the tile counts, each instance's run
 //          [start, list_end) of the infected list and its day bookkeeping.
-//   emit   one person tile per block: the infected ids, in ascending order, at
-//          their list positions.
+//   emit   one person tile per warp (per block for small runs): the infected ids,
+//          in ascending order, at their list positions.
 // Each launch depends only on the one before, so no block waits for another.
-__global__ void __launch_bounds__(kSweepThreads, 8) k_sweep_count(const InstConst *ic, InstState *is,
-                                                                  const int32_t *tile_inst, uint32_t *state,
-                                                                  uint16_t *flags_out, int32_t *tile_count,
-                                                                  const Scalars *sc, int day)
+constexpr int kSweepTilesPerBlock = 4;   // at most, person tiles a count block sweeps one after another
+
+// Adds a thread's packed status bins (and its never-infected persons, bin S of both
+// strains) into instance k's row of the day: warp reductions, one shared atomic per
+// bin per warp, one global atomic per bin per block.  Block-uniform; clears the bins.
+__device__ __forceinline__ void sweep_flush_bins(InstState *is, int k, int day, unsigned long long &bp_lo,
+                                                 unsigned long long &bp_hi, unsigned long long &bs_lo,
+                                                 unsigned long long &bs_hi, int &nss, int *s_bins)
 {
-    if (*(volatile const int *)&sc->done) return;
-    const int tile = blockIdx.x;
-    const int k = tile_inst[tile];
-    const long long tile_base = (long long)tile * kSweepTile;
-    // end of the tile's persons: none when the instance no longer runs
-    const long long N = instance_running(ic[k], is[k], day) ? (long long)ic[k].pbase + ic[k].c.N : tile_base;
-    const int d2r = day - 10;
-    // packed per-thread status bins: 16-bit fields, bins 0-3 / 4-7 per strain
-    unsigned long long bp_lo = 0, bp_hi = 0, bs_lo = 0, bs_hi = 0;
-    int nss = 0;         // persons in the never-infected state (S, S, day 255, day 255)
-    uint32_t flags = 0;  // bit (4*round + item)
-#pragma unroll
-    for (int r = 0; r < kSweepRounds; r++) {
-        long long p0 = tile_base + ((long long)r * kSweepThreads + threadIdx.x) * 4;
-        uint32_t st[4];
-        if (p0 + 3 < N) {
-            uint4 v = *reinterpret_cast<const uint4 *>(state + p0);
-            st[0] = v.x; st[1] = v.y; st[2] = v.z; st[3] = v.w;
-        } else {
-#pragma unroll
-            for (int j = 0; j < 4; j++) st[j] = (p0 + j < N) ? state[p0 + j] : 0u;
-        }
-        bool any_changed = false;
-        uint32_t out[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            // never infected by either strain: nothing to recover, bin S twice
-            if (st[j] == kNeverInfected && p0 + j < N) {
-                out[j] = st[j];
-                nss++;
-                continue;
-            }
-            bool ch;
-            out[j] = recover_word(st[j], d2r, ch);
-            if (p0 + j < N) {
-                any_changed |= ch;
-                uint32_t sp = out[j] & 0xFFu, ss = (out[j] >> 8) & 0xFFu;
-                if (sp < 4) bp_lo += 1ull << (16 * sp); else bp_hi += 1ull << (16 * (sp - 4));
-                if (ss < 4) bs_lo += 1ull << (16 * ss); else bs_hi += 1ull << (16 * (ss - 4));
-                if (sp >= 2u || ss >= 2u) flags |= 1u << (4 * r + j);
-            }
-        }
-        if (any_changed) {
-            if (p0 + 3 < N) {
-                *reinterpret_cast<uint4 *>(state + p0) = make_uint4(out[0], out[1], out[2], out[3]);
-            } else {
-#pragma unroll
-                for (int j = 0; j < 4; j++)
-                    if (p0 + j < N) state[p0 + j] = out[j];
-            }
-        }
-    }
-    flags_out[(size_t)tile * kSweepThreads + threadIdx.x] = (uint16_t)flags;
-    // status bins and the tile's infected count: warp reductions, then one atomic
-    // per bin per warp
     bp_lo += (unsigned long long)nss << 16;  // bin 1 (S) of each strain
     bs_lo += (unsigned long long)nss << 16;
-    int cnt = __popc(flags);
-    __shared__ int s_bins[17];
-    if (threadIdx.x < 17) s_bins[threadIdx.x] = 0;
-    __syncthreads();
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         bp_lo += __shfl_xor_sync(0xffffffffu, bp_lo, o);
         bp_hi += __shfl_xor_sync(0xffffffffu, bp_hi, o);
         bs_lo += __shfl_xor_sync(0xffffffffu, bs_lo, o);
         bs_hi += __shfl_xor_sync(0xffffffffu, bs_hi, o);
-        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
     }
     if ((threadIdx.x & 31) == 0) {
 #pragma unroll
@@ -999,11 +944,96 @@ __global__ void __launch_bounds__(kSweepThreads, 8) k_sweep_count(const InstCons
             if (a2) atomicAdd(&s_bins[8 + b], a2);
             if (a3) atomicAdd(&s_bins[12 + b], a3);
         }
-        if (cnt) atomicAdd(&s_bins[16], cnt);
     }
     __syncthreads();
-    if (threadIdx.x < 16 && s_bins[threadIdx.x]) atomicAdd(&is[k].counts[day][threadIdx.x], s_bins[threadIdx.x]);
-    if (threadIdx.x == 16) tile_count[tile] = s_bins[16];
+    if (threadIdx.x < 16) {
+        if (s_bins[threadIdx.x]) atomicAdd(&is[k].counts[day][threadIdx.x], s_bins[threadIdx.x]);
+        s_bins[threadIdx.x] = 0;
+    }
+    __syncthreads();
+    bp_lo = bp_hi = bs_lo = bs_hi = 0;
+    nss = 0;
+}
+
+__global__ void __launch_bounds__(kSweepThreads, 8) k_sweep_count(const InstConst *ic, InstState *is,
+                                                                  const int32_t *tile_inst, int tiles, int per_block,
+                                                                  uint32_t *state, uint16_t *flags_out,
+                                                                  int32_t *tile_count, const Scalars *sc, int day)
+{
+    if (*(volatile const int *)&sc->done) return;
+    const int t0 = blockIdx.x * per_block;
+    const int t1 = t0 + per_block < tiles ? t0 + per_block : tiles;
+    const int d2r = day - 10;
+    __shared__ int s_bins[16];
+    __shared__ int s_tc[kSweepTilesPerBlock];   // infected of each of the block's tiles
+    if (threadIdx.x < 16) s_bins[threadIdx.x] = 0;
+    if (threadIdx.x < kSweepTilesPerBlock) s_tc[threadIdx.x] = 0;
+    __syncthreads();
+    // packed per-thread status bins of the current instance: 16-bit fields, bins 0-3 /
+    // 4-7 per strain
+    unsigned long long bp_lo = 0, bp_hi = 0, bs_lo = 0, bs_hi = 0;
+    int nss = 0;         // persons in the never-infected state (S, S, day 255, day 255)
+    int cur = tile_inst[t0];
+    for (int tile = t0;; tile++) {
+        // after the last tile, or when the tiles move on to the next instance: the bins
+        const int k = tile < t1 ? tile_inst[tile] : -1;
+        if (k != cur) {
+            sweep_flush_bins(is, cur, day, bp_lo, bp_hi, bs_lo, bs_hi, nss, s_bins);  // (ends with a barrier)
+            cur = k;
+        }
+        if (k < 0) break;
+        const long long tile_base = (long long)tile * kSweepTile;
+        // end of the tile's persons: none when the instance no longer runs
+        const long long N = instance_running(ic[k], is[k], day) ? (long long)ic[k].pbase + ic[k].c.N : tile_base;
+        uint32_t flags = 0;  // bit (4*round + item)
+#pragma unroll
+        for (int r = 0; r < kSweepRounds; r++) {
+            long long p0 = tile_base + ((long long)r * kSweepThreads + threadIdx.x) * 4;
+            uint32_t st[4];
+            if (p0 + 3 < N) {
+                uint4 v = *reinterpret_cast<const uint4 *>(state + p0);
+                st[0] = v.x; st[1] = v.y; st[2] = v.z; st[3] = v.w;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) st[j] = (p0 + j < N) ? state[p0 + j] : 0u;
+            }
+            bool any_changed = false;
+            uint32_t out[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                // never infected by either strain: nothing to recover, bin S twice
+                if (st[j] == kNeverInfected && p0 + j < N) {
+                    out[j] = st[j];
+                    nss++;
+                    continue;
+                }
+                bool ch;
+                out[j] = recover_word(st[j], d2r, ch);
+                if (p0 + j < N) {
+                    any_changed |= ch;
+                    uint32_t sp = out[j] & 0xFFu, ss = (out[j] >> 8) & 0xFFu;
+                    if (sp < 4) bp_lo += 1ull << (16 * sp); else bp_hi += 1ull << (16 * (sp - 4));
+                    if (ss < 4) bs_lo += 1ull << (16 * ss); else bs_hi += 1ull << (16 * (ss - 4));
+                    if (sp >= 2u || ss >= 2u) flags |= 1u << (4 * r + j);
+                }
+            }
+            if (any_changed) {
+                if (p0 + 3 < N) {
+                    *reinterpret_cast<uint4 *>(state + p0) = make_uint4(out[0], out[1], out[2], out[3]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; j++)
+                        if (p0 + j < N) state[p0 + j] = out[j];
+                }
+            }
+        }
+        flags_out[(size_t)tile * kSweepThreads + threadIdx.x] = (uint16_t)flags;
+        int cnt = __popc(flags);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&s_tc[tile - t0], cnt);
+    }
+    if (threadIdx.x < t1 - t0) tile_count[t0 + threadIdx.x] = s_tc[threadIdx.x];
 }
 
 constexpr int kSweepScanThreads = 1024;
@@ -1072,9 +1102,11 @@ __global__ void __launch_bounds__(kSweepScanThreads) k_sweep_scan(const InstCons
     }
 }
 
-__global__ void __launch_bounds__(kSweepThreads) k_sweep_emit(const int32_t *tile_inst, const uint16_t *flags_in,
-                                                              const int32_t *tile_prefix, int32_t *infected,
-                                                              int32_t *infected_inst, const Scalars *sc)
+// Emit for small runs: a block per person tile, a block scan of the threads' packed
+// per-round counts (a warp per tile would leave most SMs idle).
+__global__ void __launch_bounds__(kSweepThreads) k_sweep_emit_block(const int32_t *tile_inst, const uint16_t *flags_in,
+                                                                    const int32_t *tile_prefix, int32_t *infected,
+                                                                    int32_t *infected_inst, const Scalars *sc)
 {
     if (*(volatile const int *)&sc->done) return;
     const int tile = blockIdx.x;
@@ -1106,6 +1138,53 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep_emit(const int32_t *til
     }
 }
 
+constexpr int kEmitWarps = 8;   // person tiles per emit block, one warp each
+
+// Emit: a warp per person tile.  Lane l reads the masks of count-kernel threads
+// 8l .. 8l+7 in one 16-byte load; per round, a warp scan of the lanes' counts places
+// them, so the ids come out in (round, thread, item) order: ascending persons.
+__global__ void __launch_bounds__(kEmitWarps * 32) k_sweep_emit(const int32_t *tile_inst, int tiles,
+                                                                const uint16_t *flags_in,
+                                                                const int32_t *tile_prefix, int32_t *infected,
+                                                                int32_t *infected_inst, const Scalars *sc)
+{
+    if (*(volatile const int *)&sc->done) return;
+    const int lane = threadIdx.x & 31;
+    const int tile = blockIdx.x * kEmitWarps + (threadIdx.x >> 5);
+    if (tile >= tiles) return;
+    const int prefix = tile_prefix[tile];
+    if (tile_prefix[tile + 1] == prefix) return;  // no infected in this tile
+    const uint4 raw = *reinterpret_cast<const uint4 *>(flags_in + (size_t)tile * kSweepThreads + 8 * lane);
+    const uint32_t wd[4] = {raw.x, raw.y, raw.z, raw.w};  // masks of threads 8l + 2i (low half), 8l + 2i + 1
+    const int k = tile_inst[tile];
+    const long long tile_base = (long long)tile * kSweepTile;
+    int round_base = prefix;
+#pragma unroll
+    for (int r = 0; r < kSweepRounds; r++) {
+        int c = 0;
+#pragma unroll
+        for (int i = 0; i < 4; i++) c += __popc((wd[i] >> (4 * r)) & 0xFu) + __popc((wd[i] >> (16 + 4 * r)) & 0xFu);
+        const int incl = warp_inclusive_scan(c);
+        int pos = round_base + incl - c;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const uint32_t m = (wd[q >> 1] >> (16 * (q & 1) + 4 * r)) & 0xFu;
+            if (m) {
+                const long long p0 = tile_base + ((long long)r * kSweepThreads + 8 * lane + q) * 4;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    if ((m >> j) & 1u) {
+                        infected[pos] = (int32_t)(p0 + j);
+                        infected_inst[pos] = k;
+                        pos++;
+                    }
+                }
+            }
+        }
+        round_base += __shfl_sync(0xffffffffu, incl, 31);
+    }
+}
+
 // The look-back control block sits right after the tile words.
 static LookBack make_lb(const DevArrays &d)
 {
@@ -1119,8 +1198,11 @@ static LookBack make_lb(const DevArrays &d)
 cudaError_t launch_sweep(const DevArrays &d, int day, cudaStream_t s)
 {
     const int tiles = d.P / kSweepTile;
-    k_sweep_count<<<tiles, kSweepThreads, 0, s>>>(d.ic, d.is, d.tile_inst, d.state, d.sweep_flags, d.sweep_tiles,
-                                                  d.sc, day);
+    // several tiles per block only where the grid still fills every SM eight times over
+    // (a small simulation keeps one tile per block and all its parallelism)
+    const int per_block = tiles >= kSweepTilesPerBlock * 8 * sm_count() ? kSweepTilesPerBlock : 1;
+    k_sweep_count<<<div_up(tiles, per_block), kSweepThreads, 0, s>>>(d.ic, d.is, d.tile_inst, tiles, per_block, d.state,
+                                                                    d.sweep_flags, d.sweep_tiles, d.sc, day);
     count_launch();
     k_sweep_scan<<<1, kSweepScanThreads, 0, s>>>(d.ic, d.is, d.K, d.sweep_tiles, tiles, d.sc, day,
                                                  d.tune.dense_level);
@@ -1131,8 +1213,13 @@ cudaError_t launch_sweep(const DevArrays &d, int day, cudaStream_t s)
 cudaError_t launch_infected_list(const DevArrays &d, cudaStream_t s)
 {
     const int tiles = d.P / kSweepTile;
-    k_sweep_emit<<<tiles, kSweepThreads, 0, s>>>(d.tile_inst, d.sweep_flags, d.sweep_tiles, d.infected,
-                                                 d.infected_inst, d.sc);
+    if (tiles >= kSweepTilesPerBlock * 8 * sm_count())
+        k_sweep_emit<<<div_up(tiles, kEmitWarps), kEmitWarps * 32, 0, s>>>(d.tile_inst, tiles, d.sweep_flags,
+                                                                           d.sweep_tiles, d.infected, d.infected_inst,
+                                                                           d.sc);
+    else
+        k_sweep_emit_block<<<tiles, kSweepThreads, 0, s>>>(d.tile_inst, d.sweep_flags, d.sweep_tiles, d.infected,
+                                                           d.infected_inst, d.sc);
     count_launch();
     return cudaGetLastError();
 }
