@@ -400,6 +400,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_radix_pass(const uint32_t *__
     // a tile of kRadixTile entries: THREADS threads, ITEMS entries each
     constexpr int WARPS = THREADS / 32, ITEMS = kRadixTile / THREADS, WARP_ITEMS = ITEMS * 32;
     static_assert(THREADS >= 256 && ITEMS * THREADS == kRadixTile, "one thread per digit and whole tiles");
+    static_assert(WARP_ITEMS <= 512, "an entry's place in its warp's digit run fits 9 bits (pack_place)");
     if (skip && *(volatile const int *)skip) return;
     __shared__ int s_tile;
     // segment, tile within it, entry base, entry count; for a dense segment of a day's
