@@ -511,7 +511,9 @@ __global__ void __launch_bounds__(THREADS, MINB) k_radix_pass(const uint32_t *__
         // phase A: rank within the warp round, per-warp digit counts.  The lanes holding
         // the same digit come from one ballot per digit bit for narrow digits, and for
         // wider ones from a shared word per digit that each lane ORs its bit into (the
-        // leader clears it again); both give the same set.
+        // leader clears it again); both give the same set.  The leader also advances the
+        // warp's count of the digit (warp_digit_before), so each entry leaves with its
+        // place among the warp's entries of its digit: earlier rounds, then lanes.
         if (nbits <= 4) {
 #pragma unroll
             for (int j = 0; j < ITEMS; j++) {
