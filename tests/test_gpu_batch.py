@@ -80,6 +80,33 @@ def test_mixed_batch_equals_standalone_runs(native_lib):
     b.close()
 
 
+# Above about 19.9M persons (four tiles per block, eight blocks per SM on 152 SMs) the
+# sweep's count blocks take four person tiles each and its emit a warp per tile; with
+# uneven instances, some count blocks span two instances and add up two bin rows.
+LARGE = [
+    (make_params(max_days=20, r_pandemic=1.8, r_seasonal=1.3, initial_pandemic=60, initial_seasonal=40,
+                 people_scaling=ps, location_scaling=10 * ps), seed)
+    for ps, seed in ((2.4, 31), (1.7, 32), (2.6, 33), (1.3, 34), (2.1, 35))
+]
+
+
+def test_large_batch_with_multi_tile_sweep_blocks_equals_standalone_runs(native_lib):
+    torch = pytest.importorskip("torch")
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    b = pt.PandemicBatch([p for p, _ in LARGE], [s for _, s in LARGE])
+    b.setup()
+    k, persons, padded = b.size()
+    if padded // 4096 < 4 * 8 * sms:
+        b.close()
+        pytest.skip("batch below the multi-tile sweep size on this GPU")
+    b.run()
+    gp, gs = b.final_gen_counts()
+    for i, (p, s) in enumerate(LARGE):
+        ref = standalone(p, s)
+        assert_instance_equal(b, i, ref, gp, gs)
+    b.close()
+
+
 def test_step_day_equals_run_and_reset_repeats(native_lib):
     params = [p for p, _ in MIXED[:4]]
     seeds = [s for _, s in MIXED[:4]]
