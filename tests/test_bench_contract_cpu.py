@@ -73,3 +73,25 @@ def test_tuning_spec_sets_named_launch_shapes_and_rejects_unknown_ones():
     assert e.tuned
     with pytest.raises(SystemExit):
         bench.apply_tuning(Engine(), "no_such_shape=3")
+
+
+def test_every_named_profile_exists_and_is_text():
+    # the ncu summaries that bench.py, the documents and the summaries themselves cite
+    import glob
+    import re
+    prof = os.path.join(ROOT, "profiles")
+    sources = [os.path.join(ROOT, f) for f in ("bench.py", "DESIGN.md", "README.md", "INTEGRATION.md")]
+    sources += glob.glob(os.path.join(ROOT, "pandemicthrust_gb300", "*.py")) + glob.glob(os.path.join(prof, "*"))
+    named = set()
+    for path in sources:
+        if not os.path.isfile(path):
+            continue
+        text = open(path, encoding="utf-8").read()
+        named.update(re.findall(r"profiles/([A-Za-z0-9_.-]+\.(?:md|txt))", text))
+        if os.path.dirname(path) == prof:
+            named.update(re.findall(r"`((?:ncu|launches)_[A-Za-z0-9_.-]+\.md)`", text))
+    assert named
+    for name in sorted(named):
+        assert os.path.isfile(os.path.join(prof, name)), name
+    for path in glob.glob(os.path.join(prof, "*")):
+        assert path.endswith((".md", ".txt")), path
